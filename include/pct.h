@@ -1,0 +1,155 @@
+/*
+ * pct_gb300 — C ABI of the GB300-native proton-CT reconstruction path.
+ *
+ * Drop-in boundary for the reconstruction hot path of lynch829/pCT: history
+ * preprocessing (binning, statistical cuts, sinogram), SC/MSC/SM hulls, FBP,
+ * MLP hull endpoints and voxel rows, and the DROP block solver.  The reference
+ * exposes that path as void entry points over global arrays
+ * (include/pCT_functions.h:37-237); this ABI carries the same stages over a
+ * context that owns all device memory and one CUDA stream.
+ *
+ * Conventions
+ *   - Every call returns pct_status; nothing calls exit().  pct_last_error()
+ *     gives a message for the calling thread's last failure.
+ *   - Host buffers belong to the caller; device buffers belong to the context.
+ *     Entry points that take device pointers say so ("device pointer").
+ *   - One context is used by one host thread at a time.  Independent contexts
+ *     may run concurrently.
+ *   - Units are cm and radians inside the library; the history upload takes
+ *     the PCTD file layout (mm, degrees) like read_data_chunk_v02
+ *     (src/pCT_Reconstruction_Data_Segments.cu:1769-1933).
+ */
+#ifndef PCT_H
+#define PCT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pct_status {
+    PCT_OK = 0,
+    PCT_ERR_ARGUMENT = 1,   /* bad pointer, size or configuration value */
+    PCT_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    PCT_ERR_ALLOC = 3,      /* device or host allocation failed */
+    PCT_ERR_STATE = 4,      /* stage called out of order */
+    PCT_ERR_OVERFLOW = 5,   /* a fixed-capacity buffer or counter would overflow */
+    PCT_ERR_TIMEOUT = 6,    /* a bounded device-side wait gave up */
+    PCT_ERR_IO = 7,         /* file read/write failed or malformed PCTD data */
+    PCT_ERR_NUMERIC = 8     /* non-finite value where the algorithm needs a number */
+} pct_status;
+
+/* Hull and initial-iterate choices, same values as the reference enums
+ * HULL_TYPES, INITIAL_ITERATE and FILTER_TYPES (include/pCT_data.h:245,292,357). */
+enum { PCT_SC_HULL = 0, PCT_MSC_HULL = 1, PCT_SM_HULL = 2, PCT_FBP_HULL = 3 };
+enum { PCT_X_HULL = 0, PCT_FBP_IMAGE = 1, PCT_HYBRID = 2, PCT_ZEROS = 3, PCT_IMPORT = 4 };
+enum { PCT_RAM_LAK = 0, PCT_SHEPP_LOGAN = 1, PCT_NO_FILTER = 2 };
+
+/*
+ * Run-time configuration.  Every field is a compile-time constant of the
+ * reference; pct_config_default() returns the reference header values
+ * (include/pCT_config.h, include/pCT_data.h:215-420).  Derived sizes
+ * (SLICES, T_BINS, NUM_VOXELS, ...) are computed from these exactly as the
+ * reference macros do.
+ */
+typedef struct pct_config {
+    /* scanner and binning (pCT_data.h:222-244) */
+    double source_radius;          /* SOURCE_RADIUS [cm] */
+    double gantry_angle_interval;  /* GANTRY_ANGLE_INTERVAL [deg] */
+    double ssd_t_size;             /* SSD_T_SIZE [cm] */
+    double ssd_v_size;             /* SSD_V_SIZE [cm] */
+    double t_bin_size;             /* T_BIN_SIZE [cm] */
+    double v_bin_size;             /* V_BIN_SIZE [cm] */
+    double angular_bin_size;       /* ANGULAR_BIN_SIZE [deg] */
+    int sigmas_to_keep;            /* SIGMAS_TO_KEEP */
+    int sample_std_dev;            /* SAMPLE_STD_DEV (pCT_config.h:18) */
+    /* reconstruction volume (pCT_data.h:255-277) */
+    double recon_cyl_radius;       /* RECON_CYL_RADIUS [cm] */
+    int columns;                   /* COLUMNS */
+    int rows;                      /* ROWS */
+    double slice_thickness;        /* SLICE_THICKNESS [cm] */
+    /* hulls (pCT_config.h:23-26, pCT_data.h:281-293) */
+    int sc_on, msc_on, sm_on;      /* SC_ON, MSC_ON, SM_ON */
+    int avg_filter_hull;           /* AVG_FILTER_HULL */
+    int mlp_hull;                  /* MLP_HULL: PCT_*_HULL */
+    int msc_diff_thresh;           /* MSC_DIFF_THRESH */
+    double sc_threshold;           /* SC_THRESHOLD [cm] */
+    double msc_threshold;          /* MSC_THRESHOLD [cm] */
+    double sm_lower_threshold;     /* SM_LOWER_THRESHOLD [cm] */
+    double sm_scale_threshold;     /* SM_SCALE_THRESHOLD */
+    double hull_filter_threshold;  /* HULL_FILTER_THRESHOLD */
+    int hull_filter_radius;        /* HULL_FILTER_RADIUS */
+    /* FBP (pCT_data.h:245-251, pCT_config.h:19) */
+    int fbp_on;                    /* FBP_ON */
+    int fbp_filter;                /* FBP_FILTER: PCT_RAM_LAK / PCT_SHEPP_LOGAN / PCT_NO_FILTER */
+    double fbp_threshold;          /* FBP_THRESHOLD */
+    /* iterative reconstruction (pCT_config.h:5, pCT_data.h:358-377) */
+    int x_k0;                      /* X_K0: PCT_X_HULL ... */
+    int iterations;                /* ITERATIONS */
+    int block_size;                /* BLOCK_SIZE_RECON */
+    float lambda;                  /* LAMBDA */
+    /* GB300 extensions (no reference counterpart) */
+    double residual_tol;           /* stop DROP early when the FP64 relative data
+                                      residual falls below this (0: run all iterations) */
+    int chord_bf16;                /* store per-row chord lengths in bf16 (0: fp32) */
+} pct_config;
+
+/* Geometry derived from a pct_config, as the reference macros derive it. */
+typedef struct pct_geometry {
+    int columns, rows, slices, num_voxels;
+    int t_bins, v_bins, angular_bins, num_bins, gantry_angles;
+    double recon_cyl_radius, recon_cyl_height;
+    double voxel_width, voxel_height, voxel_thickness;
+    double x_zero, y_zero, z_zero;
+    double mlp_u_step;
+} pct_geometry;
+
+/* ---- synthetic phantoms and histories (no reference counterpart) ------- */
+enum { PCT_PRIM_CYLINDER = 0, PCT_PRIM_ELLIPSOID = 1 };
+/* One phantom primitive; RSP values of overlapping primitives add.
+ * Cylinder: axis along z through (cx, cy), radius a, |z - cz| <= c.
+ * Ellipsoid: center (cx, cy, cz), semi-axes a, b, c, rotated by phi about z. */
+typedef struct pct_phantom_object {
+    int kind;
+    double cx, cy, cz;
+    double a, b, c;
+    double phi;
+    double rsp;
+} pct_phantom_object;
+
+typedef struct pct_scan_params {
+    uint64_t seed;
+    int num_angles;                /* gantry angles, histories split evenly, angle-major */
+    double gantry_angle_interval;  /* [deg] */
+    double t_extent, v_extent;     /* half-width / half-height of the field at isocenter [cm] */
+    double source_radius;          /* fan divergence source distance [cm] */
+    double angular_spread;         /* Gaussian beam spread [rad] */
+    double beam_energy_mev;        /* kinetic energy, 200 */
+    double wepl_noise;             /* relative Gaussian WEPL noise, 0.02 */
+    double outlier_fraction;       /* fraction of object-hitting histories with uniform WEPL */
+    double outlier_max;            /* upper bound of the uniform outlier WEPL [cm] */
+    double scatter_scale;          /* multiplier on the Highland width */
+} pct_scan_params;
+
+/* Fills the 13 PCTD arrays (t0..t3, v0..v3, u0..u3, WEPL; mm) and the
+ * per-history projection angle [deg] for n histories. */
+pct_status pct_generate_histories(const pct_phantom_object* objs, int n_objs, const pct_scan_params* sp,
+                                  float* const out[13], float* projection_angle, int64_t n);
+/* RSP of the phantom averaged over supersample^3 points per voxel, in the
+ * voxel order of the reconstruction (column fastest, slice 0 at z = +H/2). */
+pct_status pct_phantom_voxelize(const pct_phantom_object* objs, int n_objs, const pct_config* cfg,
+                                int supersample, float* image);
+
+pct_status pct_config_default(pct_config* cfg);
+pct_status pct_geometry_from_config(const pct_config* cfg, pct_geometry* geo);
+const char* pct_last_error(void);
+const char* pct_status_string(pct_status s);
+/* sizeof of ABI structs (0 config, 1 geometry, 2 phantom object, 3 scan params, ...). */
+size_t pct_sizeof(int which);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PCT_H */

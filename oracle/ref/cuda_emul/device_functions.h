@@ -1,0 +1,2 @@
+/* Emulation stub: the real declarations come from pct_ref_prelude.h (test infrastructure only). */
+#include "pct_ref_prelude.h"

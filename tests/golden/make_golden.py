@@ -1,0 +1,121 @@
+#!/usr/bin/env python3
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+For each scenario below: seeded synthetic histories (pct_gb300.phantoms) are
+written as PCTD v0 files, the reference's own driver sequence runs on them
+(oracle/refharness.py: the unmodified reference source compiled for the host
+by oracle/build_ref.py, main()'s call order), and every stage output is
+stored.  MLP voxel rows come from the reference's find_MLP_path_GPU
+(src/pCT_Reconstruction_Data_Segments.cu:5279) run on the recon histories.
+
+Needs the reference checkout (default /root/reference), so it runs in the
+development container only; the fixtures are committed.  Large arrays are
+stored as SHA-256 digests plus a leading sample, small ones in full.
+
+    python tests/golden/make_golden.py [--ref /root/reference] [scenario ...]
+"""
+import argparse
+import ctypes as C
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from pct_gb300 import pctd, phantoms  # noqa: E402
+from oracle import refharness  # noqa: E402
+
+FULL_LIMIT = 20000      # arrays up to this many elements are stored in full
+SAMPLE = 512            # leading elements kept for larger arrays
+
+
+def scenarios():
+    return {
+        # z-clip branches of the intersection code and MLP rows that leave the slab
+        "tiny_clip": dict(geometry="tiny", workload=phantoms.tiny(num_histories=40000, seed=11, v_extent=0.55),
+                          run=dict(msc_on=1, mlp_hull=1, iterations=0), mlp_rows=4000),
+        # in-slab scan through DROP (2 iterations, block 6000, lambda 0.1)
+        "tiny_drop": dict(geometry="tiny", workload=phantoms.tiny(num_histories=40000, seed=7, v_extent=0.3),
+                          run=dict(msc_on=1, mlp_hull=1, iterations=2, block_size=6000, lambda_=0.1), mlp_rows=4000),
+        # 200x200x8 water-cylinder geometry with the SM hull
+        "cfg1_sm": dict(geometry="cfg1", workload=phantoms.cfg1(num_histories=120000, seed=5),
+                        run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=0), mlp_rows=1500),
+    }
+
+
+def digest(a):
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def pack(name, arr, out):
+    out["dtype:" + name] = np.array(str(arr.dtype))
+    out["shape:" + name] = np.array(arr.shape, dtype=np.int64)
+    out["sha:" + name] = np.array(digest(arr))
+    if arr.size <= FULL_LIMIT:
+        out["full:" + name] = arr
+    else:
+        out["head:" + name] = arr.ravel()[:SAMPLE]
+
+
+def mlp_rows_reference(geometry, res, limit):
+    lib = refharness.load(geometry)
+    n = min(limit, len(res["recon.x_entry"]))
+    x = np.zeros(1 << 22, np.float32)
+    path = np.zeros(1 << 14, np.uint32)
+    rows, offsets, chord = [], [0], []
+    for i in range(n):
+        inp = np.array([res["recon." + f][i] for f in ("x_entry", "y_entry", "z_entry", "x_exit", "y_exit", "z_exit",
+                                                      "xy_entry_angle", "xz_entry_angle", "xy_exit_angle",
+                                                      "xz_exit_angle", "WEPL")], np.float32)
+        ch, ad, aa = C.c_double(), C.c_double(), C.c_double()
+        k = lib.pctref_mlp_path_gpu(x.ctypes.data, inp.ctypes.data, int(res["recon.first_MLP_voxel"][i]),
+                                    path.ctypes.data, C.byref(ch), C.byref(ad), C.byref(aa))
+        rows.append(path[:k].copy())
+        offsets.append(offsets[-1] + k)
+        chord.append(ch.value)
+    return np.concatenate(rows), np.array(offsets, np.int64), np.array(chord, np.float64)
+
+
+def make(name, sc, ref_root):
+    refharness.ensure_built(sc["geometry"], ref_root)
+    w = sc["workload"]
+    data, angles = phantoms.generate(w)
+    with tempfile.TemporaryDirectory() as tmp:
+        pctd.write_scan(tmp, "scan", data, angles, w.num_angles, w.gantry_angle_interval)
+        res = refharness.run_pipeline(sc["geometry"], os.path.join(tmp, "ref.npz"), input_directory=tmp + "/",
+                                      input_folder="scan", **sc["run"])
+    if int(res["__rc"][0]) != 0:
+        raise SystemExit("%s: reference run returned %d" % (name, int(res["__rc"][0])))
+    rows, offsets, chord = mlp_rows_reference(sc["geometry"], res, sc["mlp_rows"])
+    res["mlp.rows"], res["mlp.offsets"], res["mlp.chord"] = rows, offsets, chord
+    out = {"scenario": np.array(name), "workload": np.array(w.name), "seed": np.array(w.seed),
+           "num_histories": np.array(w.num_histories), "v_extent": np.array(w.v_extent),
+           "input_sha": np.array(digest(data) + digest(angles)),
+           "run_config": np.array(repr(sc["run"]))}
+    for k, v in res.items():
+        if k.startswith("__"):
+            continue
+        pack(k, v, out)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print("%s: %d arrays, %d bytes" % (path, len(res), os.path.getsize(path)))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("names", nargs="*")
+    a = ap.parse_args()
+    sc = scenarios()
+    for name in (a.names or sorted(sc)):
+        make(name, sc[name], a.ref)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+"""Pins the CPU oracle to the reference's own outputs (tests/golden/*.npz).
+
+The fixtures were produced by tests/golden/make_golden.py: the unmodified
+reference driver sequence run on seeded synthetic PCTD scans.  Here the oracle
+runs the same scans with sequential binary32 bin sums (the order in which the
+fixture run added them) and must reproduce every stage bit for bit; the DROP
+iterates, which the reference keeps in binary32, must match the oracle's
+binary64 run within 1e-6 relative L2.
+"""
+import glob
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from pct_gb300 import phantoms
+from oracle import oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1}
+DROP_TOL = 1e-6
+
+
+def load_fixture(path):
+    with np.load(path, allow_pickle=False) as z:
+        return {k: z[k] for k in z.files}
+
+
+def workload_of(fx):
+    kw = dict(num_histories=int(fx["num_histories"]), seed=int(fx["seed"]))
+    if str(fx["workload"]) == "tiny":
+        kw["v_extent"] = float(fx["v_extent"])
+    return WORKLOADS[str(fx["workload"])](**kw)
+
+
+def run_kwargs(fx):
+    return eval(str(fx["run_config"]), {"__builtins__": {}})
+
+
+def names(fx):
+    return sorted(k[4:] for k in fx if k.startswith("sha:"))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def oracle_outputs(fx):
+    w = workload_of(fx)
+    data, angles = phantoms.generate(w)
+    assert sha(data) + sha(angles) == str(fx["input_sha"]), "synthetic inputs differ from the fixture's"
+    cfg = phantoms.make_config(w.config)
+    run = run_kwargs(fx)
+    for k in ("msc_on", "sm_on", "sc_on", "mlp_hull"):
+        if k in run:
+            setattr(cfg, k, run[k])
+    out = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_SEQUENTIAL, iterations=run.get("iterations", 0),
+                              block_size=run.get("block_size", 3200), lam=float(np.float32(run.get("lambda_", 0.001))),
+                              keep_history=True)
+    # names of the reference captures that the oracle produces under another name
+    out["x_0"] = out["x_k0"]
+    out["bin_counts_pre"] = out["bin_counts_post"]
+    if "sha:mlp.rows" in fx:
+        n = int(fx["shape:mlp.chord"][0])
+        if "mlp.rows" not in out:
+            hr = {k: v[:n] for k, v in out["_hr"].items()}
+            out["mlp.offsets"], out["mlp.rows"], out["mlp.chord"] = oracle.mlp_rows(cfg, hr)
+        out["mlp.offsets"] = out["mlp.offsets"][: n + 1]
+        out["mlp.rows"] = out["mlp.rows"][: out["mlp.offsets"][-1]]
+        out["mlp.chord"] = out["mlp.chord"][:n]
+    return cfg, out
+
+
+@pytest.fixture(scope="module", params=FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+def case(request):
+    fx = load_fixture(request.param)
+    cfg, out = oracle_outputs(fx)
+    return fx, cfg, out
+
+
+EXACT_SKIP = {"x_final", "sinogram_pre"}
+
+
+def test_every_stage_bit_exact(case):
+    fx, cfg, out = case
+    checked, bad = 0, []
+    for name in names(fx):
+        if name in EXACT_SKIP or (name.startswith("x_") and name[2:].isdigit() and name != "x_0"):
+            continue
+        if name not in out:
+            continue
+        a = np.asarray(out[name])
+        want_dtype = str(fx["dtype:" + name])
+        a = a.astype(want_dtype) if str(a.dtype) != want_dtype and a.dtype.kind != "f" else a
+        if str(a.dtype) != want_dtype:
+            a = a.astype(want_dtype)
+        if tuple(a.shape) != tuple(fx["shape:" + name]) or sha(a) != str(fx["sha:" + name]):
+            bad.append(name)
+        checked += 1
+    assert checked >= 60, "too few stages compared (%d)" % checked
+    assert not bad, "stages differ from the reference: %s" % bad
+
+
+def test_drop_iterates_within_tolerance(case):
+    fx, cfg, out = case
+    its = [k for k in names(fx) if k.startswith("x_") and k[2:].isdigit() and k != "x_0"]
+    if not its:
+        pytest.skip("scenario stops before DROP")
+    for k in its:
+        ref = fx["full:" + k].astype(np.float64)
+        err = np.linalg.norm(out[k] - ref) / np.linalg.norm(ref)
+        assert err <= DROP_TOL, "%s: relative L2 %.3e" % (k, err)
+
+
+def test_walk_guards_never_fire(case):
+    """The oracle caps walks the reference leaves unbounded; on these inputs the caps must stay idle."""
+    fx, cfg, out = case
+    for k in ("msc_walk_stats", "sm_walk_stats"):
+        if k in out:
+            assert out[k][0] == 0, "%s capped %d walks" % (k, out[k][0])
+    assert int(out["endpoint_walks_capped"][0]) == 0
