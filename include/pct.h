@@ -142,6 +142,96 @@ pct_status pct_generate_histories(const pct_phantom_object* objs, int n_objs, co
 pct_status pct_phantom_voxelize(const pct_phantom_object* objs, int n_objs, const pct_config* cfg,
                                 int supersample, float* image);
 
+/* ---- reconstruction context ------------------------------------------- */
+typedef struct pct_ctx pct_ctx;
+
+/* History counts after each stage (the reference's total_histories,
+ * recon_vol_histories, post_cut_histories, reconstruction_histories;
+ * include/pCT_data.h:474-478, 367). */
+typedef struct pct_counts {
+    int64_t total_histories;
+    int64_t recon_vol_histories;
+    int64_t post_cut_histories;
+    int64_t reconstruction_histories;
+    int64_t row_entries;             /* MLP row entries over all recon histories */
+    int64_t rows_outside_image;      /* row entries whose voxel index lies outside the image */
+    int64_t walks_capped;            /* hull/endpoint walks stopped by the step cap */
+    int64_t mlp_fp64_samples;        /* MLP samples recomputed in FP64 near a voxel face */
+} pct_counts;
+
+/* Per-iteration DROP statistics (GB300 extension). */
+typedef struct pct_drop_stats {
+    int iterations_run;
+    double residual[64];             /* FP64 relative data residual ||b - A x|| / ||b|| before each iteration, and after the last */
+    double seconds;                  /* device time of the iterations */
+} pct_drop_stats;
+
+/* Arrays readable with pct_get_array().  H_* are per-history arrays of the
+ * current history store (compacted in place after binning, cuts and
+ * endpoints, like the reference's *_vector globals, pCT_data.h:577-595). */
+typedef enum pct_array {
+    PCT_ARR_MSC_COUNTS = 0, PCT_ARR_SM_COUNTS, PCT_ARR_SC_HULL, PCT_ARR_MSC_HULL, PCT_ARR_SM_HULL,   /* int32 voxels */
+    PCT_ARR_BIN_COUNTS_PRE, PCT_ARR_MEAN_WEPL, PCT_ARR_MEAN_UT, PCT_ARR_MEAN_UV,                    /* bins */
+    PCT_ARR_SD_WEPL, PCT_ARR_SD_UT, PCT_ARR_SD_UV, PCT_ARR_BIN_COUNTS_POST, PCT_ARR_SINOGRAM,
+    PCT_ARR_SINOGRAM_FILTERED,
+    PCT_ARR_FBP_IMAGE, PCT_ARR_FBP_HULL, PCT_ARR_X_HULL, PCT_ARR_X_HULL_FILTERED, PCT_ARR_X0, PCT_ARR_X, /* voxels */
+    PCT_ARR_H_BIN_NUM, PCT_ARR_H_WEPL, PCT_ARR_H_X_ENTRY, PCT_ARR_H_Y_ENTRY, PCT_ARR_H_Z_ENTRY,         /* histories */
+    PCT_ARR_H_X_EXIT, PCT_ARR_H_Y_EXIT, PCT_ARR_H_Z_EXIT, PCT_ARR_H_XY_ENTRY_ANGLE, PCT_ARR_H_XZ_ENTRY_ANGLE,
+    PCT_ARR_H_XY_EXIT_ANGLE, PCT_ARR_H_XZ_EXIT_ANGLE, PCT_ARR_H_FIRST_VOXEL, PCT_ARR_H_FAILED_CUTS,
+    PCT_ARR_ROW_OFFSETS, PCT_ARR_ROWS, PCT_ARR_CHORD,                                                  /* MLP rows */
+    PCT_ARR_COUNT
+} pct_array;
+
+/* Creates a context on CUDA device `device`; every buffer it owns lives there. */
+pct_status pct_create(const pct_config* cfg, int device, pct_ctx** out);
+pct_status pct_destroy(pct_ctx* ctx);
+/* Capacity hint for the history store (total histories to be uploaded). */
+pct_status pct_reserve(pct_ctx* ctx, int64_t total_histories);
+
+/* One chunk of PCTD histories: unit conversion, cylinder intersections,
+ * binning and the hull walks.  Replaces read_data_chunk + recon_volume_intersections
+ * + binning + hull_detection (pCT_functions.h:37,44,45,61;
+ * src/pCT_Reconstruction_Data_Segments.cu:97-100).  data13 are the 13 PCTD
+ * arrays (t0..t3, v0..v3, u0..u3, WEPL; mm), projection_angle the header
+ * angle of each history [deg].  Pointers are host memory unless
+ * data_on_device is nonzero (then device pointers on the context's device). */
+pct_status pct_process_chunk(pct_ctx* ctx, const float* const data13[13], const float* projection_angle, int64_t n,
+                             int data_on_device);
+/* hull_detection_finish (pCT_functions.h:62): MSC/SM edge detection. */
+pct_status pct_hull_detection_finish(pct_ctx* ctx);
+/* calculate_means, sum_squared_deviations, calculate_standard_deviations,
+ * statistical_cuts and construct_sinogram (pCT_functions.h:46-52). */
+pct_status pct_statistical_cuts(pct_ctx* ctx);
+/* FBP (pCT_functions.h:53): filter, backprojection, FBP hull. */
+pct_status pct_fbp(pct_ctx* ctx);
+/* hull_selection (pCT_functions.h:69) including the averaging filter. */
+pct_status pct_hull_selection(pct_ctx* ctx);
+/* define_initial_iterate (pCT_functions.h:85).  For PCT_IMPORT, x0 is taken
+ * from pct_set_image() beforehand. */
+pct_status pct_define_initial_iterate(pct_ctx* ctx);
+/* reconstruction_cuts (pCT_functions.h:230): hull entry/exit of each history,
+ * compaction to the histories that cross the hull. */
+pct_status pct_collect_mlp_endpoints(pct_ctx* ctx);
+/* MLP voxel rows of every recon history, kept resident for all iterations. */
+pct_status pct_mlp_rows(pct_ctx* ctx);
+/* DROP iterations on the resident rows (the iteration loop of
+ * image_reconstruction_GPU, src/pCT_Reconstruction_Data_Segments.cu:6795-6860).
+ * stats may be NULL. */
+pct_status pct_drop(pct_ctx* ctx, int iterations, pct_drop_stats* stats);
+/* image_reconstruction_GPU (pCT_functions.h:237): endpoints, rows, all
+ * cfg->iterations DROP iterations. */
+pct_status pct_image_reconstruction(pct_ctx* ctx, pct_drop_stats* stats);
+
+pct_status pct_get_counts(pct_ctx* ctx, pct_counts* counts);
+/* Copies an array to host memory; *bytes is the capacity in, the size out. */
+pct_status pct_get_array(pct_ctx* ctx, pct_array which, void* host_dst, size_t* bytes);
+/* Device pointer and byte size of an array (valid until the next stage call). */
+pct_status pct_array_device_ptr(pct_ctx* ctx, pct_array which, void** dptr, size_t* bytes);
+/* Replaces the current iterate (host pointer, num_voxels floats). */
+pct_status pct_set_image(pct_ctx* ctx, const float* x);
+/* CUDA stream the context runs on (cudaStream_t). */
+void* pct_stream(pct_ctx* ctx);
+
 pct_status pct_config_default(pct_config* cfg);
 pct_status pct_geometry_from_config(const pct_config* cfg, pct_geometry* geo);
 const char* pct_last_error(void);

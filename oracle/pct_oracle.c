@@ -173,8 +173,10 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
         int t_bin = pct_d2i((t / cfg->t_bin_size) + T2);
         double v = z_mid;
         int v_bin = pct_d2i((v / cfg->v_bin_size) + V2);
-        if ((t_bin >= 0) && (v_bin >= 0) && (t_bin < g.t_bins) && (v_bin < g.v_bins)) {
-            bin_num[i] = t_bin + angle_bin * g.t_bins + v_bin * g.t_bins * g.angular_bins;
+        int bin = t_bin + angle_bin * g.t_bins + v_bin * g.t_bins * g.angular_bins;
+        /* a negative angle bin (NaN path angle) would index outside the bins; treated as invalid */
+        if ((t_bin >= 0) && (v_bin >= 0) && (t_bin < g.t_bins) && (v_bin < g.v_bins) && bin >= 0 && bin < g.num_bins) {
+            bin_num[i] = bin;
             bin_valid[i] = 1;
         } else {
             bin_num[i] = 0;
@@ -864,7 +866,10 @@ static int64_t mlp_path(const pct_geometry* g, double x_in, double y_in, double 
     double pre1 = u_2 * u_2 * u_2 * (AL(0, 3) + u_2 * (AL(1, 12) + u_2 * (AL(2, 30) + u_2 * (AL(3, 60) + u_2 * (AL(4, 105) + AU(u_2, 5, 168))))));
     double pre2 = u_2 * u_2 * (AL(0, 2) + u_2 * (AL(1, 6) + u_2 * (AL(2, 12) + u_2 * (AL(3, 20) + u_2 * (AL(4, 30) + AU(u_2, 5, 42))))));
     double pre3 = u_2 * (A0 + u_2 * (AL(1, 2) + u_2 * (AL(2, 3) + u_2 * (AL(3, 4) + u_2 * (AL(4, 5) + AU(u_2, 5, 6))))));
+    const int cap = 8 * (g->columns + g->rows + g->slices) + 64;
+    int steps = 0;
     while (u_1 < u_2 - STEP) {
+        if (++steps > cap) break; /* non-finite endpoints only */
         R0[1] = u_1;
         R1[1] = u_2 - u_1;
         R1T[2] = u_2 - u_1;

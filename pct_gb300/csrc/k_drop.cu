@@ -1,0 +1,214 @@
+/*
+ * Stages a16-a18: the DROP block-iterative solver on resident MLP rows.
+ *
+ * Per block of B consecutive recon histories (BLOCK_SIZE_RECON, the
+ * reference's block loop .cu:6803-6844):
+ *   k_drop_rows   block_update_GPU (.cu:5774-5841) without the MLP: one warp per
+ *                 row gathers x over the row (the iterate at the start of the
+ *                 block), forms the update c * lambda * (b - c sum x) / ||a||^2
+ *                 with ||a||^2 in binary64, and adds it to every voxel of the row
+ *                 (float reductions into L2-resident x_update); it also adds the
+ *                 squared residual of the row to a binary64 accumulator.
+ *   k_drop_relax  image_update_GPU (.cu:5900-5938): x += x_update / s_j where s_j
+ *                 is the number of block rows through voxel j (the DROP diagonal
+ *                 weight); s_j is fixed by the rows and the block split, so it is
+ *                 counted once (k_block_counts) instead of in every iteration.
+ * One CUDA graph holds the 2 * blocks launches of an iteration.
+ */
+#include <cstring>
+#include "pct_device.cuh"
+
+namespace {
+
+constexpr int DROP_THREADS = 256;
+constexpr int DROP_WARPS = DROP_THREADS / 32;
+
+__global__ void k_block_counts(int64_t start, int64_t end, const int64_t* __restrict__ off,
+                               const uint32_t* __restrict__ rows, uint32_t nv, uint32_t* __restrict__ cnt) {
+    int64_t p0 = off[start], p1 = off[end];
+    for (int64_t p = p0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t v = rows[p];
+        if (v < nv) atomicAdd(cnt + v, 1u);
+    }
+}
+
+__global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64_t end,
+                                                            const int64_t* __restrict__ off,
+                                                            const uint32_t* __restrict__ rows,
+                                                            const float* __restrict__ chord,
+                                                            const double* __restrict__ inv_norm,
+                                                            const float* __restrict__ wepl, float lambda,
+                                                            const float* __restrict__ x, float* __restrict__ upd,
+                                                            uint32_t nv, double* __restrict__ resid) {
+    __shared__ double sres[DROP_WARPS];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t i = start + (int64_t)blockIdx.x * DROP_WARPS + w;
+    double r2 = 0.0;
+    if (i < end) {
+        int64_t a = off[i], b = off[i + 1];
+        float dot = 0.0f;
+        for (int64_t p = a + lane; p < b; p += 32) {
+            uint32_t v = rows[p];
+            if (v < nv) dot += x[v];
+        }
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        double c = chord[i];
+        double res = (double)wepl[i] - c * (double)dot;
+        float value = (float)(c * res * inv_norm[i] * (double)lambda);
+        for (int64_t p = a + lane; p < b; p += 32) {
+            uint32_t v = rows[p];
+            if (v < nv) atomicAdd(upd + v, value);
+        }
+        r2 = res * res;
+    }
+    if (lane == 0) sres[w] = r2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < DROP_WARPS; ++k) s += sres[k];
+        if (s != 0.0) atomicAdd(resid, s);
+    }
+}
+
+__global__ void k_drop_relax(int nv, const uint32_t* __restrict__ cnt, float* __restrict__ x, float* __restrict__ upd) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    uint32_t s = cnt[v];
+    if (s > 0) {
+        x[v] += upd[v] / (float)s;
+        upd[v] = 0.0f;
+    }
+}
+
+/* Moves the iteration's residual accumulator into its history slot. */
+__global__ void k_store_resid(double* __restrict__ acc, double* __restrict__ slot) {
+    *slot = *acc;
+    *acc = 0.0;
+}
+
+__global__ void k_wepl_norm(int64_t n, const float* __restrict__ wepl, double* __restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double w = wepl[i];
+        s += w * w;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+        atomicAdd(out, t);
+    }
+}
+
+}  // namespace
+
+static pct_status build_block_counts(pct_ctx* c) {
+    const int64_t n = c->h.n;
+    const int64_t B = c->cfg.block_size;
+    const int nv = c->geo.num_voxels;
+    int nb = (int)((n + B - 1) / B);
+    PCT_TRY(c->block_diag.alloc(sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1)));
+    PCT_CUDA(cudaMemsetAsync(c->block_diag.p, 0, sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
+    for (int k = 0; k < nb; ++k) {
+        int64_t s = k * B, e = s + B < n ? s + B : n;
+        k_block_counts<<<1216, 256, 0, c->stream>>>(s, e, c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(),
+                                                    (uint32_t)nv, c->block_diag.as<uint32_t>() + (size_t)k * nv);
+    }
+    PCT_CUDA(cudaGetLastError());
+    c->num_blocks = nb;
+    c->diag_ready = 1;
+    return PCT_OK;
+}
+
+/* Enqueues one DROP iteration (all blocks) on the context stream. */
+static void enqueue_iteration(pct_ctx* c, double* resid) {
+    const int64_t n = c->h.n;
+    const int64_t B = c->cfg.block_size;
+    const int nv = c->geo.num_voxels;
+    for (int k = 0; k < c->num_blocks; ++k) {
+        int64_t s = k * B, e = s + B < n ? s + B : n;
+        unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
+        k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(),
+                                                          c->chord.as<float>(), c->inv_norm.as<double>(),
+                                                          c->h.wepl.as<float>(), c->cfg.lambda, c->x.as<float>(),
+                                                          c->x_update.as<float>(), (uint32_t)nv, resid);
+        k_drop_relax<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(nv, c->block_diag.as<uint32_t>() + (size_t)k * nv,
+                                                                   c->x.as<float>(), c->x_update.as<float>());
+    }
+}
+
+static pct_status capture_iteration(pct_ctx* c, double* acc) {
+    if (c->drop_graph_exec) return PCT_OK;
+    cudaGraph_t graph = nullptr;
+    PCT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_iteration(c, acc);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess) return pct_fail(PCT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return pct_fail(PCT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    c->drop_graph_exec = exec;
+    return PCT_OK;
+}
+
+pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
+    if (c->stage != ST_ROWS) return pct_fail(PCT_ERR_STATE, "drop needs MLP rows");
+    if (iterations < 0) return pct_fail(PCT_ERR_ARGUMENT, "drop: negative iteration count");
+    const int nv = c->geo.num_voxels;
+    if (!c->diag_ready) {
+        PCT_TRY(build_block_counts(c));
+        pct_drop_release_graph(c);
+    }
+    PCT_TRY(c->x_update.alloc(sizeof(float) * nv));
+    PCT_CUDA(cudaMemsetAsync(c->x_update.p, 0, sizeof(float) * nv, c->stream));
+    const int maxit = 64;
+    /* [0, maxit): per-iteration squared residual, maxit: accumulator, maxit+1: ||b||^2 */
+    PCT_TRY(c->drop_resid.alloc(sizeof(double) * (maxit + 2)));
+    double* d_res = c->drop_resid.as<double>();
+    PCT_CUDA(cudaMemsetAsync(d_res, 0, sizeof(double) * (maxit + 2), c->stream));
+    if (c->h.n > 0) k_wepl_norm<<<304, 256, 0, c->stream>>>(c->h.n, c->h.wepl.as<float>(), d_res + maxit + 1);
+    PCT_TRY(capture_iteration(c, d_res + maxit));
+    cudaEvent_t e0, e1;
+    PCT_CUDA(cudaEventCreate(&e0));
+    PCT_CUDA(cudaEventCreate(&e1));
+    PCT_CUDA(cudaEventRecord(e0, c->stream));
+    int done = 0;
+    double res_host[maxit + 2];
+    for (int it = 0; it < iterations; ++it) {
+        PCT_CUDA(cudaGraphLaunch(c->drop_graph_exec, c->stream));
+        k_store_resid<<<1, 1, 0, c->stream>>>(d_res + maxit, d_res + (it < maxit ? it : maxit - 1));
+        ++done;
+        if (c->cfg.residual_tol > 0.0) {
+            PCT_CUDA(cudaMemcpyAsync(res_host, d_res, sizeof(double) * (maxit + 2), cudaMemcpyDeviceToHost, c->stream));
+            PCT_CUDA(cudaStreamSynchronize(c->stream));
+            double b2 = res_host[maxit + 1];
+            double rel = b2 > 0 ? sqrt(res_host[it < maxit ? it : maxit - 1] / b2) : 0.0;
+            if (rel < c->cfg.residual_tol) break;
+        }
+    }
+    PCT_CUDA(cudaEventRecord(e1, c->stream));
+    PCT_CUDA(cudaGetLastError());
+    PCT_CUDA(cudaMemcpyAsync(res_host, d_res, sizeof(double) * (maxit + 2), cudaMemcpyDeviceToHost, c->stream));
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations_run = done;
+        double b2 = res_host[maxit + 1];
+        for (int k = 0; k < done && k < maxit; ++k) stats->residual[k] = b2 > 0 ? sqrt(res_host[k] / b2) : 0.0;
+        stats->seconds = ms * 1e-3;
+    }
+    return PCT_OK;
+}
+
+void pct_drop_release_graph(pct_ctx* c) {
+    if (c->drop_graph_exec) cudaGraphExecDestroy(c->drop_graph_exec);
+    c->drop_graph_exec = nullptr;
+}

@@ -1,0 +1,397 @@
+/*
+ * Stages a1-a6 of the path: unit conversion, reconstruction-cylinder
+ * intersections, binning, per-bin statistics, 3-sigma cuts and the sinogram.
+ *
+ *   k_preprocess    one thread per history, fused a1+a2+a3 and the first
+ *                   statistics pass (read_data_chunk_v02 conversion .cu:1883-1921,
+ *                   recon_volume_intersections_GPU .cu:2169-2387, binning_GPU
+ *                   .cu:2507-2578).  SoA in, SoA out; per-bin sums go to exact
+ *                   int64 fixed-point accumulators (order independent), where the
+ *                   reference adds binary32 atomics in arbitrary order.
+ *   k_means, k_sq_dev, k_sigma   calculate_means_GPU, sum_squared_deviations_GPU,
+ *                   calculate_standard_deviations_GPU (.cu:2618-2730)
+ *   k_cuts, k_sinogram           statistical_cuts_GPU, construct_sinogram_GPU
+ *                   (.cu:2835-2917)
+ * HBM-bound streaming kernels except k_preprocess, which is bound by binary64
+ * arithmetic (a few hundred flops per history on a part with little FP64).
+ */
+#include "pct_device.cuh"
+
+namespace {
+
+struct In13 {
+    const float* p[13];
+};
+
+/* calculate_intercepts (.cu:2301-2387); outputs are zero when the line misses. */
+__device__ int dev_intercepts(const DevGeom& g, double u, double t, double ut_angle, double* ui, double* ti) {
+    int cone = ((ut_angle > PCT_PI_OVER_4) && (ut_angle < PCT_THREE_PI_OVER_4)) ||
+               ((ut_angle > PCT_FIVE_PI_OVER_4) && (ut_angle < PCT_SEVEN_PI_OVER_4));
+    double tmp;
+    *ui = 0.0;
+    *ti = 0.0;
+    if (cone) {
+        tmp = u;
+        u = -t;
+        t = tmp;
+        ut_angle += PCT_PI_OVER_2;
+    }
+    double m = pct_tan(ut_angle);
+    double b_in = t - m * u;
+    double a = 1 + m * m;
+    double b = 2 * m * b_in;
+    double c = b_in * b_in - g.recon_cyl_radius * g.recon_cyl_radius;
+    double disc = b * b - (4 * a * c);
+    int hit = disc > 0;
+    if (hit) {
+        double sq = sqrt(disc);
+        double u1 = (sq - b) / (2 * a);
+        double u2 = (sq + b) / (2 * a);
+        double t1 = m * u1 + b_in;
+        double t2 = m * u2 - b_in;
+        double d1 = (u1 - u) * (u1 - u) + (t1 - t) * (t1 - t);
+        double d2 = (u2 + u) * (u2 + u) + (t2 + t) * (t2 + t);
+        *ui = u1 * (d1 <= d2) - u2 * (d1 > d2);
+        *ti = t1 * (d1 <= d2) - t2 * (d1 > d2);
+    }
+    if (cone) {
+        tmp = *ui;
+        *ui = *ti;
+        *ti = -tmp;
+    }
+    return hit;
+}
+
+__device__ __forceinline__ int dev_sgn(float z) { return (z >= 0) - (z < 0); }
+
+__global__ void k_trig_table(double2* __restrict__ out, int n, double a, double b) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        double ang = (i * a) * b;
+        out[i] = make_double2(pct_cos(ang), pct_sin(ang));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_preprocess(DevGeom g, In13 in, const float* __restrict__ proj, int64_t n,
+                                                    const double2* __restrict__ trig_gantry,
+                                                    const double2* __restrict__ trig_bins, HistView out,
+                                                    uint8_t* __restrict__ missed, int* __restrict__ counts,
+                                                    long long* __restrict__ sum1, int angular_bin_deg_div) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    /* a1 (.cu:1883-1897, 1921) */
+    float t_in_1 = (float)((double)in.p[0][i] * PCT_MM_TO_CM), t_in_2 = (float)((double)in.p[1][i] * PCT_MM_TO_CM);
+    float t_out_1 = (float)((double)in.p[2][i] * PCT_MM_TO_CM), t_out_2 = (float)((double)in.p[3][i] * PCT_MM_TO_CM);
+    float v_in_1 = (float)((double)in.p[4][i] * PCT_MM_TO_CM), v_in_2 = (float)((double)in.p[5][i] * PCT_MM_TO_CM);
+    float v_out_1 = (float)((double)in.p[6][i] * PCT_MM_TO_CM), v_out_2 = (float)((double)in.p[7][i] * PCT_MM_TO_CM);
+    float u_in_1 = (float)((double)in.p[8][i] * PCT_MM_TO_CM), u_in_2 = (float)((double)in.p[9][i] * PCT_MM_TO_CM);
+    float u_out_1 = (float)((double)in.p[10][i] * PCT_MM_TO_CM), u_out_2 = (float)((double)in.p[11][i] * PCT_MM_TO_CM);
+    float w = (float)((double)in.p[12][i] * PCT_MM_TO_CM);
+    int ga = ((int)proj[i] + 270) % 360;
+    /* a2 (.cu:2198-2298) */
+    double rot = ga * PCT_ANGLE_TO_RADIANS;
+    double2 cs = (ga >= 0 && ga < 360) ? trig_gantry[ga] : make_double2(pct_cos(rot), pct_sin(rot));
+    double cr = cs.x, sr = cs.y;
+    double ut_entry = pct_atan2f(t_in_2 - t_in_1, u_in_2 - u_in_1);
+    double u_e, t_e, u_x, t_x;
+    int entered = dev_intercepts(g, u_in_2, t_in_2, ut_entry, &u_e, &t_e);
+    float xy_in = (float)(ut_entry + rot);
+    float xe = (float)((cr * u_e) - (sr * t_e));
+    float ye = (float)((sr * u_e) + (cr * t_e));
+    double ut_exit = pct_atan2f(t_out_2 - t_out_1, u_out_2 - u_out_1);
+    int exited = dev_intercepts(g, u_out_1, t_out_1, ut_exit, &u_x, &t_x);
+    float xy_out = (float)(ut_exit + rot);
+    float xx = (float)((cr * u_x) - (sr * t_x));
+    float yx = (float)((sr * u_x) + (cr * t_x));
+    double uv_entry_slope = (double)((v_in_2 - v_in_1) / (u_in_2 - u_in_1));
+    double uv_exit_slope = (double)((v_out_2 - v_out_1) / (u_out_2 - u_out_1));
+    float xz_in = pct_atan2f(v_in_2 - v_in_1, u_in_2 - u_in_1);
+    float xz_out = pct_atan2f(v_out_2 - v_out_1, u_out_2 - u_out_1);
+    u_e = (cr * xe) + (sr * ye);
+    u_x = (cr * xx) + (sr * yx);
+    float ze = (float)(v_in_2 + uv_entry_slope * (u_e - u_in_2));
+    float zx = (float)(v_out_1 - uv_exit_slope * (u_out_1 - u_x));
+    const double H = g.recon_cyl_height;
+    if (entered && exited) {
+        if ((fabsf(ze) < H * 0.5) && (fabsf(zx) > H * 0.5)) {
+            double f = fabs((dev_sgn(zx) * H * 0.5 - ze) / (zx - ze));
+            xx = (float)(xe + f * (xx - xe));
+            yx = (float)(ye + f * (yx - ye));
+            zx = (float)(dev_sgn(zx) * H * 0.5);
+        } else if (fabsf(ze) > H * 0.5) {
+            entered = 0;
+            exited = 0;
+        }
+        if ((fabsf(ze) > H * 0.5) && (fabsf(zx) < H * 0.5)) {
+            double f = fabs((dev_sgn(zx) * H * 0.5 - zx) / (zx - ze));
+            xe = (float)(xx + f * (xx - xe));
+            ye = (float)(yx + f * (yx - ye));
+            ze = (float)(dev_sgn(ze) * H * 0.5);
+        }
+        if ((fabsf(t_out_1 - t_in_2) > 5) || (fabsf(v_out_1 - v_in_2) > 5)) {
+            entered = 0;
+            exited = 0;
+        }
+    }
+    uint8_t m = !entered || !exited;
+    /* a3 (.cu:2529-2550) */
+    double x_mid = (xe + xx) / 2;
+    double y_mid = (ye + yx) / 2;
+    double z_mid = (ze + zx) / 2;
+    double path_angle = pct_atan2f(yx - ye, xx - xe);
+    if (path_angle < 0) path_angle += 2 * PCT_PI;
+    int angle_bin = pct_d2i((path_angle * PCT_RADIANS_TO_ANGLE / g.angular_bin_size) + 0.5) % g.angular_bins;
+    double2 ab;
+    if (angle_bin >= 0 && angle_bin < g.angular_bins) {
+        ab = trig_bins[angle_bin];
+    } else {
+        double angle = angle_bin * g.angular_bin_size * PCT_ANGLE_TO_RADIANS;
+        ab = make_double2(pct_cos(angle), pct_sin(angle));
+    }
+    double t = y_mid * ab.x - x_mid * ab.y;
+    int t_bin = pct_d2i((t / g.t_bin_size) + (g.t_bins / 2));
+    int v_bin = pct_d2i((z_mid / g.v_bin_size) + (g.v_bins / 2));
+    int valid = (t_bin >= 0) && (v_bin >= 0) && (t_bin < g.t_bins) && (v_bin < g.v_bins);
+    int bin = valid ? t_bin + angle_bin * g.t_bins + v_bin * g.t_bins * g.angular_bins : 0;
+    /* a negative angle bin (NaN path angle) would index outside the bins */
+    if (bin < 0 || bin >= g.num_bins) {
+        valid = 0;
+        bin = 0;
+    }
+    out.x_entry[i] = xe; out.y_entry[i] = ye; out.z_entry[i] = ze;
+    out.x_exit[i] = xx; out.y_exit[i] = yx; out.z_exit[i] = zx;
+    out.xy_entry_angle[i] = xy_in; out.xz_entry_angle[i] = xz_in;
+    out.xy_exit_angle[i] = xy_out; out.xz_exit_angle[i] = xz_out;
+    out.wepl[i] = w;
+    out.bin_num[i] = bin;
+    out.bin_valid[i] = (uint8_t)valid;
+    out.failed[i] = 0;
+    out.first_voxel[i] = 0;
+    missed[i] = m;
+    /* binning sums (.cu:2551-2570) */
+    if (!m && valid) {
+        float rut = (float)dev_rel_angle(xy_out, xy_in);
+        float ruv = (float)dev_rel_angle(xz_out, xz_in);
+        atomicAdd(counts + bin, 1);
+        dev_add_fixed(sum1 + 3 * (int64_t)bin + 0, dev_to_fixed(w, PCT_SCALE_WEPL));
+        dev_add_fixed(sum1 + 3 * (int64_t)bin + 1, dev_to_fixed(rut, PCT_SCALE_ANGLE));
+        dev_add_fixed(sum1 + 3 * (int64_t)bin + 2, dev_to_fixed(ruv, PCT_SCALE_ANGLE));
+    }
+}
+
+/* calculate_means_GPU (.cu:2618-2627) on the exact sums */
+__global__ void k_means(int nb, const int* __restrict__ counts, const long long* __restrict__ sum1,
+                        float* __restrict__ mw, float* __restrict__ mut, float* __restrict__ muv) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    float a = dev_from_fixed(sum1[3 * (int64_t)b + 0], PCT_SCALE_WEPL);
+    float u = dev_from_fixed(sum1[3 * (int64_t)b + 1], PCT_SCALE_ANGLE);
+    float v = dev_from_fixed(sum1[3 * (int64_t)b + 2], PCT_SCALE_ANGLE);
+    int c = counts[b];
+    if (c > 0) {
+        a /= c;
+        u /= c;
+        v /= c;
+    }
+    mw[b] = a;
+    mut[b] = u;
+    muv[b] = v;
+}
+
+/* sum_squared_deviations_GPU (.cu:2678-2698): every kept history, bin 0 included */
+__global__ void __launch_bounds__(256) k_sq_dev(int64_t n, HistView h, const float* __restrict__ mw,
+                                                const float* __restrict__ mut, const float* __restrict__ muv,
+                                                long long* __restrict__ sum2) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int b = h.bin_num[i];
+    double rut = dev_rel_angle(h.xy_exit_angle[i], h.xy_entry_angle[i]);
+    double ruv = dev_rel_angle(h.xz_exit_angle[i], h.xz_entry_angle[i]);
+    double dw = h.wepl[i] - mw[b];
+    double dut = rut - mut[b];
+    double duv = ruv - muv[b];
+    dev_add_fixed(sum2 + 3 * (int64_t)b + 0, dev_to_fixed((float)(dw * dw), PCT_SCALE_WEPL));
+    dev_add_fixed(sum2 + 3 * (int64_t)b + 1, dev_to_fixed((float)(dut * dut), PCT_SCALE_ANGLE_SQ));
+    dev_add_fixed(sum2 + 3 * (int64_t)b + 2, dev_to_fixed((float)(duv * duv), PCT_SCALE_ANGLE_SQ));
+}
+
+/* calculate_standard_deviations_GPU (.cu:2718-2730); also clears the counts
+ * for the post-cut recount like the reference (.cu:2730). */
+__global__ void k_sigma(int nb, const int* __restrict__ counts, const long long* __restrict__ sum2, int sample,
+                        float* __restrict__ sw, float* __restrict__ sut, float* __restrict__ suv) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    float a = dev_from_fixed(sum2[3 * (int64_t)b + 0], PCT_SCALE_WEPL);
+    float u = dev_from_fixed(sum2[3 * (int64_t)b + 1], PCT_SCALE_ANGLE_SQ);
+    float v = dev_from_fixed(sum2[3 * (int64_t)b + 2], PCT_SCALE_ANGLE_SQ);
+    int c = counts[b];
+    if (c > 1) {
+        int div = c - sample;
+        a = sqrtf(a / div);
+        u = sqrtf(u / div);
+        v = sqrtf(v / div);
+    }
+    sw[b] = a;
+    sut[b] = u;
+    suv[b] = v;
+}
+
+/* statistical_cuts_GPU (.cu:2844-2868); keep[i] = passed */
+__global__ void __launch_bounds__(256) k_cuts(int64_t n, HistView h, int K, const float* __restrict__ mw,
+                                              const float* __restrict__ mut, const float* __restrict__ muv,
+                                              const float* __restrict__ sw, const float* __restrict__ sut,
+                                              const float* __restrict__ suv, uint8_t* __restrict__ keep,
+                                              int* __restrict__ counts_post, long long* __restrict__ sino_sum) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int b = h.bin_num[i];
+    double rut = dev_rel_angle(h.xy_exit_angle[i], h.xy_entry_angle[i]);
+    double ruv = dev_rel_angle(h.xz_exit_angle[i], h.xz_entry_angle[i]);
+    float w = h.wepl[i];
+    int p_ut = fabs(rut - mut[b]) < (K * sut[b]);
+    int p_uv = fabs(ruv - muv[b]) < (K * suv[b]);
+    int p_w = fabsf(mw[b] - w) <= (K * sw[b]);
+    int f = !p_ut || !p_uv || !p_w;
+    h.failed[i] = (uint8_t)f;
+    keep[i] = (uint8_t)!f;
+    if (!f) {
+        atomicAdd(counts_post + b, 1);
+        dev_add_fixed(sino_sum + b, dev_to_fixed(w, PCT_SCALE_WEPL));
+    }
+}
+
+/* construct_sinogram_GPU (.cu:2912-2917) */
+__global__ void k_sinogram(int nb, const int* __restrict__ counts_post, const long long* __restrict__ sino_sum,
+                           float* __restrict__ sino) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    float s = dev_from_fixed(sino_sum[b], PCT_SCALE_WEPL);
+    if (counts_post[b] > 0) s /= counts_post[b];
+    sino[b] = s;
+}
+
+}  // namespace
+
+pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed);  /* k_hull.cu */
+
+namespace {
+__global__ void k_invert(const uint8_t* __restrict__ a, uint8_t* __restrict__ b, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = !a[i];
+}
+}  // namespace
+
+static pct_status pct_invert_flags(pct_ctx* c, const uint8_t* a, uint8_t* b, int64_t n) {
+    k_invert<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(a, b, n);
+    PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
+
+static pct_status ensure_tables(pct_ctx* c) {
+    if (c->trig_gantry.p) return PCT_OK;
+    PCT_TRY(c->trig_gantry.alloc(sizeof(double2) * 360));
+    PCT_TRY(c->trig_bins.alloc(sizeof(double2) * c->geo.angular_bins));
+    k_trig_table<<<2, 256, 0, c->stream>>>(c->trig_gantry.as<double2>(), 360, 1.0, PCT_ANGLE_TO_RADIANS);
+    k_trig_table<<<pct_grid_for(c->geo.angular_bins, 256), 256, 0, c->stream>>>(
+        c->trig_bins.as<double2>(), c->geo.angular_bins, c->cfg.angular_bin_size, PCT_ANGLE_TO_RADIANS);
+    PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
+
+static pct_status ensure_bins(pct_ctx* c) {
+    if (c->bin_counts.p) return PCT_OK;
+    size_t nb = (size_t)c->geo.num_bins;
+    PCT_TRY(c->bin_counts.alloc(nb * 4));
+    PCT_TRY(c->bin_counts_post.alloc(nb * 4));
+    PCT_TRY(c->bin_sum1.alloc(nb * 3 * 8));
+    PCT_TRY(c->bin_sum2.alloc(nb * 3 * 8));
+    PCT_TRY(c->sino_sum.alloc(nb * 8));
+    DevBuf* f[] = {&c->mean_wepl, &c->mean_ut, &c->mean_uv, &c->sd_wepl, &c->sd_ut, &c->sd_uv, &c->sinogram,
+                   &c->sinogram_filtered};
+    for (DevBuf* b : f) PCT_TRY(b->alloc(nb * 4));
+    PCT_CUDA(cudaMemsetAsync(c->bin_counts.p, 0, nb * 4, c->stream));
+    PCT_CUDA(cudaMemsetAsync(c->bin_sum1.p, 0, nb * 3 * 8, c->stream));
+    return PCT_OK;
+}
+
+pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], const float* angle, int64_t n,
+                                   int on_dev) {
+    if (c->stage > ST_BINNED) return pct_fail(PCT_ERR_STATE, "process_chunk after hull_detection_finish");
+    if (n == 0) {
+        c->stage = ST_BINNED;
+        return PCT_OK;
+    }
+    PCT_TRY(ensure_tables(c));
+    PCT_TRY(ensure_bins(c));
+    In13 in;
+    const float* d_angle = angle;
+    if (!on_dev) {
+        for (int k = 0; k < 13; ++k) {
+            PCT_TRY(c->in13[k].alloc(sizeof(float) * n));
+            PCT_CUDA(cudaMemcpyAsync(c->in13[k].p, data13[k], sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+            in.p[k] = c->in13[k].as<float>();
+        }
+        PCT_TRY(c->in_angle.alloc(sizeof(float) * n));
+        PCT_CUDA(cudaMemcpyAsync(c->in_angle.p, angle, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+        d_angle = c->in_angle.as<float>();
+    } else {
+        for (int k = 0; k < 13; ++k) in.p[k] = data13[k];
+    }
+    PCT_TRY(c->h2.reserve(n, c->stream));
+    PCT_TRY(c->tmp_missed.alloc(n * 2));
+    uint8_t* missed = c->tmp_missed.as<uint8_t>();
+    uint8_t* keep = missed + n;
+    HistView stage = c->view(c->h2);
+    k_preprocess<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(
+        c->dg, in, d_angle, n, c->trig_gantry.as<double2>(), c->trig_bins.as<double2>(), stage, missed,
+        c->bin_counts.as<int>(), c->bin_sum1.as<long long>(), 0);
+    PCT_CUDA(cudaGetLastError());
+    /* hull detection runs on the whole chunk (.cu:100) */
+    PCT_TRY(pct_hull_walk_chunk(c, n, missed));
+    /* keep = !missed (bin_num >= 0 always holds, .cu:2446) */
+    PCT_TRY(pct_invert_flags(c, missed, keep, n));
+    int64_t kept = 0;
+    PCT_TRY(c->h.reserve(c->h.n + n, c->stream));
+    PCT_TRY(pct_compact(c, c->h2, 0, n, keep, c->h, c->h.n, &kept));
+    c->h.n += kept;
+    c->counts.total_histories += n;
+    c->counts.recon_vol_histories += kept;
+    c->stage = ST_BINNED;
+    return PCT_OK;
+}
+
+pct_status pct_stage_cuts(pct_ctx* c) {
+    if (c->stage < ST_BINNED) return pct_fail(PCT_ERR_STATE, "statistical_cuts before any chunk");
+    if (c->stage >= ST_CUT) return pct_fail(PCT_ERR_STATE, "statistical_cuts already done");
+    PCT_TRY(ensure_bins(c));
+    const int nb = c->geo.num_bins;
+    const int64_t n = c->h.n;
+    HistView h = c->view(c->h);
+    k_means<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts.as<int>(), c->bin_sum1.as<long long>(),
+                                                          c->mean_wepl.as<float>(), c->mean_ut.as<float>(),
+                                                          c->mean_uv.as<float>());
+    PCT_CUDA(cudaMemsetAsync(c->bin_sum2.p, 0, (size_t)nb * 3 * 8, c->stream));
+    if (n > 0)
+        k_sq_dev<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, h, c->mean_wepl.as<float>(), c->mean_ut.as<float>(),
+                                                               c->mean_uv.as<float>(), c->bin_sum2.as<long long>());
+    k_sigma<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts.as<int>(), c->bin_sum2.as<long long>(),
+                                                          c->cfg.sample_std_dev ? 1 : 0, c->sd_wepl.as<float>(),
+                                                          c->sd_ut.as<float>(), c->sd_uv.as<float>());
+    PCT_CUDA(cudaMemsetAsync(c->bin_counts_post.p, 0, (size_t)nb * 4, c->stream));
+    PCT_CUDA(cudaMemsetAsync(c->sino_sum.p, 0, (size_t)nb * 8, c->stream));
+    PCT_TRY(c->tmp_missed.alloc(n > 0 ? n : 1));
+    uint8_t* keep = c->tmp_missed.as<uint8_t>();
+    if (n > 0)
+        k_cuts<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(
+            n, h, c->cfg.sigmas_to_keep, c->mean_wepl.as<float>(), c->mean_ut.as<float>(), c->mean_uv.as<float>(),
+            c->sd_wepl.as<float>(), c->sd_ut.as<float>(), c->sd_uv.as<float>(), keep, c->bin_counts_post.as<int>(),
+            c->sino_sum.as<long long>());
+    k_sinogram<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts_post.as<int>(),
+                                                             c->sino_sum.as<long long>(), c->sinogram.as<float>());
+    PCT_CUDA(cudaGetLastError());
+    int64_t kept = 0;
+    PCT_TRY(pct_compact_histories(c, keep, n, &kept));
+    c->counts.post_cut_histories = kept;
+    c->stage = ST_CUT;
+    return PCT_OK;
+}

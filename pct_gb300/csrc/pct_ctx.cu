@@ -1,0 +1,441 @@
+/*
+ * Context lifetime, device buffers, array getters and the stable history
+ * compaction shared by the stages.
+ */
+#include <cstring>
+#include <utility>
+#include "pct_ctx.h"
+
+pct_status DevBuf::alloc(size_t n) {
+    if (n <= bytes && p) return PCT_OK;
+    release();
+    if (n == 0) return PCT_OK;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cudaGetLastError();
+        return pct_fail(PCT_ERR_ALLOC, "cudaMalloc(%zu bytes): %s", n, cudaGetErrorString(e));
+    }
+    bytes = n;
+    return PCT_OK;
+}
+
+pct_status DevBuf::grow_keep(size_t n, cudaStream_t s) {
+    if (n <= bytes && p) return PCT_OK;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return pct_fail(PCT_ERR_ALLOC, "cudaMalloc(%zu bytes): %s", n, cudaGetErrorString(e));
+    }
+    if (p && bytes) {
+        e = cudaMemcpyAsync(q, p, bytes, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            cudaFree(q);
+            return pct_fail(PCT_ERR_CUDA, "grow_keep copy: %s", cudaGetErrorString(e));
+        }
+    }
+    release();
+    p = q;
+    bytes = n;
+    return PCT_OK;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+pct_status HistoryStore::reserve(int64_t cap, cudaStream_t s) {
+    if (cap <= capacity) return PCT_OK;
+    size_t f = sizeof(float) * (size_t)cap;
+    DevBuf* fl[] = {&x_entry, &y_entry, &z_entry, &x_exit, &y_exit, &z_exit,
+                    &xy_entry_angle, &xz_entry_angle, &xy_exit_angle, &xz_exit_angle, &wepl, &bin_num, &first_voxel};
+    for (DevBuf* b : fl) PCT_TRY(b->grow_keep(f, s));
+    PCT_TRY(bin_valid.grow_keep((size_t)cap, s));
+    PCT_TRY(failed.grow_keep((size_t)cap, s));
+    capacity = cap;
+    return PCT_OK;
+}
+
+void HistoryStore::release() {
+    DevBuf* all[] = {&x_entry, &y_entry, &z_entry, &x_exit, &y_exit, &z_exit, &xy_entry_angle, &xz_entry_angle,
+                     &xy_exit_angle, &xz_exit_angle, &wepl, &bin_num, &bin_valid, &failed, &first_voxel};
+    for (DevBuf* b : all) b->release();
+    n = capacity = 0;
+}
+
+HistView pct_ctx::view(HistoryStore& s) const {
+    HistView v;
+    v.x_entry = s.x_entry.as<float>(); v.y_entry = s.y_entry.as<float>(); v.z_entry = s.z_entry.as<float>();
+    v.x_exit = s.x_exit.as<float>(); v.y_exit = s.y_exit.as<float>(); v.z_exit = s.z_exit.as<float>();
+    v.xy_entry_angle = s.xy_entry_angle.as<float>(); v.xz_entry_angle = s.xz_entry_angle.as<float>();
+    v.xy_exit_angle = s.xy_exit_angle.as<float>(); v.xz_exit_angle = s.xz_exit_angle.as<float>();
+    v.wepl = s.wepl.as<float>();
+    v.bin_num = s.bin_num.as<int32_t>();
+    v.bin_valid = s.bin_valid.as<uint8_t>();
+    v.failed = s.failed.as<uint8_t>();
+    v.first_voxel = s.first_voxel.as<uint32_t>();
+    return v;
+}
+
+DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g) {
+    DevGeom d;
+    d.columns = g.columns; d.rows = g.rows; d.slices = g.slices; d.num_voxels = g.num_voxels;
+    d.t_bins = g.t_bins; d.v_bins = g.v_bins; d.angular_bins = g.angular_bins; d.num_bins = g.num_bins;
+    d.recon_cyl_radius = g.recon_cyl_radius; d.recon_cyl_height = g.recon_cyl_height;
+    d.voxel_width = g.voxel_width; d.voxel_height = g.voxel_height; d.voxel_thickness = g.voxel_thickness;
+    d.x_zero = g.x_zero; d.y_zero = g.y_zero; d.z_zero = g.z_zero; d.mlp_u_step = g.mlp_u_step;
+    d.t_bin_size = c.t_bin_size; d.v_bin_size = c.v_bin_size; d.angular_bin_size = c.angular_bin_size;
+    d.gantry_angle_interval = c.gantry_angle_interval; d.source_radius = c.source_radius;
+    d.slice_thickness = c.slice_thickness;
+    return d;
+}
+
+/* ---- stable compaction ------------------------------------------------------ */
+namespace {
+constexpr int CT_THREADS = 256;
+constexpr int CT_ITEMS = 8;
+constexpr int CT_TILE = CT_THREADS * CT_ITEMS;
+
+__global__ void k_tile_counts(const uint8_t* __restrict__ keep, int64_t n, int* __restrict__ tile_counts) {
+    int64_t base = (int64_t)blockIdx.x * CT_TILE;
+    int c = 0;
+    for (int k = 0; k < CT_ITEMS; ++k) {
+        int64_t i = base + (int64_t)k * CT_THREADS + threadIdx.x;
+        if (i < n && keep[i]) ++c;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    __shared__ int ws[CT_THREADS / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < CT_THREADS / 32; ++w) t += ws[w];
+        tile_counts[blockIdx.x] = t;
+    }
+}
+
+/* Single-block exclusive scan of the tile counts; writes the total after them. */
+__global__ void k_scan_tiles(int* __restrict__ tile_counts, int64_t* __restrict__ tile_offsets, int tiles,
+                             int64_t* __restrict__ total) {
+    __shared__ int64_t carry;
+    __shared__ int64_t ws[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < tiles; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int64_t v = i < tiles ? tile_counts[i] : 0;
+        int64_t x = v;
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int64_t s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            ws[lane] = s;
+        }
+        __syncthreads();
+        int64_t incl = x + (w > 0 ? ws[w - 1] : 0);
+        if (i < tiles) tile_offsets[i] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+struct CompactArgs {
+    const void* src[16];
+    void* dst[16];
+    int size[16];
+    int nfields;
+};
+
+__global__ void k_scatter(const uint8_t* __restrict__ keep, int64_t n, const int64_t* __restrict__ tile_offsets,
+                          CompactArgs a) {
+    __shared__ int ws[CT_THREADS / 32 + 1];
+    int64_t base = (int64_t)blockIdx.x * CT_TILE;
+    int64_t out = tile_offsets[blockIdx.x];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < CT_ITEMS; ++k) {
+        int64_t i = base + (int64_t)k * CT_THREADS + threadIdx.x;
+        bool f = i < n && keep[i];
+        unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) ws[w] = __popc(m);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int j = 0; j < CT_THREADS / 32; ++j) {
+            if (j < w) before += ws[j];
+            total += ws[j];
+        }
+        int pos = before + __popc(m & ((1u << lane) - 1));
+        if (f) {
+            int64_t d = out + pos;
+            for (int q = 0; q < a.nfields; ++q) {
+                if (a.size[q] == 4) ((uint32_t*)a.dst[q])[d] = ((const uint32_t*)a.src[q])[i];
+                else ((uint8_t*)a.dst[q])[d] = ((const uint8_t*)a.src[q])[i];
+            }
+        }
+        out += total;
+        __syncthreads();
+    }
+}
+}  // namespace
+
+pct_status pct_compact(pct_ctx* c, HistoryStore& src, int64_t src_off, int64_t n, const uint8_t* d_keep,
+                       HistoryStore& dst, int64_t dst_off, int64_t* kept) {
+    *kept = 0;
+    if (n == 0) return PCT_OK;
+    int64_t tiles = (n + CT_TILE - 1) / CT_TILE;
+    PCT_TRY(c->scan_tmp.alloc(tiles * (sizeof(int) + sizeof(int64_t)) + 64));
+    int* tile_counts = c->scan_tmp.as<int>();
+    int64_t* tile_offsets = (int64_t*)((char*)c->scan_tmp.p + ((tiles * sizeof(int) + 15) & ~(size_t)15));
+    PCT_TRY(c->pinned_count.alloc(sizeof(int64_t) * 2));
+    int64_t* d_total = c->pinned_count.as<int64_t>();
+    PCT_TRY(dst.reserve(dst_off + n, c->stream));
+    k_tile_counts<<<(unsigned)tiles, CT_THREADS, 0, c->stream>>>(d_keep, n, tile_counts);
+    k_scan_tiles<<<1, 1024, 0, c->stream>>>(tile_counts, tile_offsets, (int)tiles, d_total);
+    CompactArgs a;
+    DevBuf* sf[] = {&src.x_entry, &src.y_entry, &src.z_entry, &src.x_exit, &src.y_exit, &src.z_exit,
+                    &src.xy_entry_angle, &src.xz_entry_angle, &src.xy_exit_angle, &src.xz_exit_angle, &src.wepl,
+                    &src.bin_num, &src.first_voxel, &src.bin_valid, &src.failed};
+    DevBuf* df[] = {&dst.x_entry, &dst.y_entry, &dst.z_entry, &dst.x_exit, &dst.y_exit, &dst.z_exit,
+                    &dst.xy_entry_angle, &dst.xz_entry_angle, &dst.xy_exit_angle, &dst.xz_exit_angle, &dst.wepl,
+                    &dst.bin_num, &dst.first_voxel, &dst.bin_valid, &dst.failed};
+    a.nfields = 15;
+    for (int q = 0; q < 15; ++q) {
+        int sz = q < 13 ? 4 : 1;
+        a.src[q] = (const char*)sf[q]->p + src_off * sz;
+        a.dst[q] = (char*)df[q]->p + dst_off * sz;
+        a.size[q] = sz;
+    }
+    k_scatter<<<(unsigned)tiles, CT_THREADS, 0, c->stream>>>(d_keep, n, tile_offsets, a);
+    PCT_CUDA(cudaGetLastError());
+    int64_t total = 0;
+    PCT_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    *kept = total;
+    return PCT_OK;
+}
+
+pct_status pct_compact_histories(pct_ctx* c, const uint8_t* d_keep, int64_t n, int64_t* kept) {
+    PCT_TRY(pct_compact(c, c->h, 0, n, d_keep, c->h2, 0, kept));
+    std::swap(c->h, c->h2);
+    c->h.n = *kept;
+    return PCT_OK;
+}
+
+/* ---- C ABI: lifetime and getters ---------------------------------------------- */
+extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** out) {
+    if (!cfg || !out) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: null argument");
+    *out = nullptr;
+    pct_geometry g;
+    int e = pct_geometry_derive(cfg, &g);
+    if (e) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: invalid geometry (code %d)", e);
+    if (cfg->block_size <= 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: block_size must be positive");
+    if (cfg->mlp_hull < 0 || cfg->mlp_hull > 3) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: bad mlp_hull");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return pct_fail(PCT_ERR_CUDA, "pct_create: no CUDA device");
+    }
+    if (device < 0 || device >= ndev) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: device %d of %d", device, ndev);
+    pct_ctx* c = new pct_ctx();
+    c->cfg = *cfg;
+    c->geo = g;
+    c->dg = pct_make_devgeom(*cfg, g);
+    c->device = device;
+    pct_status s = c->set_device();
+    if (s == PCT_OK) {
+        cudaError_t ce = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (ce != cudaSuccess) s = pct_fail(PCT_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(ce));
+    }
+    if (s == PCT_OK) s = c->err_flags.alloc(sizeof(unsigned long long) * ERR_COUNT);
+    if (s == PCT_OK && cudaMemsetAsync(c->err_flags.p, 0, c->err_flags.bytes, c->stream) != cudaSuccess)
+        s = pct_fail(PCT_ERR_CUDA, "memset err flags");
+    if (s != PCT_OK) {
+        pct_destroy(c);
+        return s;
+    }
+    *out = c;
+    return PCT_OK;
+}
+
+extern "C" pct_status pct_destroy(pct_ctx* c) {
+    if (!c) return PCT_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf* all[] = {&c->in_angle, &c->tmp_missed, &c->tmp_hist, &c->scan_tmp, &c->pinned_count, &c->bin_counts,
+                     &c->bin_counts_post, &c->bin_sum1, &c->bin_sum2, &c->sino_sum, &c->mean_wepl, &c->mean_ut,
+                     &c->mean_uv, &c->sd_wepl, &c->sd_ut, &c->sd_uv, &c->sinogram, &c->sinogram_filtered,
+                     &c->filter_taps, &c->filter_scale, &c->trig_gantry, &c->trig_bins, &c->err_flags,
+                     &c->sc_hull, &c->msc_counts, &c->sm_counts, &c->msc_hull, &c->sm_hull, &c->fbp_image,
+                     &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
+                     &c->rows, &c->chord, &c->inv_norm, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
+                     &c->drop_resid};
+    for (DevBuf* b : all) b->release();
+    for (auto& b : c->in13) b.release();
+    pct_drop_release_graph(c);
+    c->h.release();
+    c->h2.release();
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return PCT_OK;
+}
+
+extern "C" pct_status pct_reserve(pct_ctx* c, int64_t total) {
+    if (!c || total < 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_reserve: bad argument");
+    PCT_TRY(c->set_device());
+    return c->h.reserve(total, c->stream);
+}
+
+extern "C" void* pct_stream(pct_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" pct_status pct_get_counts(pct_ctx* c, pct_counts* out) {
+    if (!c || !out) return pct_fail(PCT_ERR_ARGUMENT, "pct_get_counts: null argument");
+    PCT_TRY(c->set_device());
+    unsigned long long f[ERR_COUNT];
+    PCT_CUDA(cudaMemcpyAsync(f, c->err_flags.p, sizeof(f), cudaMemcpyDeviceToHost, c->stream));
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    *out = c->counts;
+    out->walks_capped = (int64_t)f[ERR_WALK_CAPPED];
+    out->mlp_fp64_samples = (int64_t)f[ERR_MLP_FP64];
+    out->rows_outside_image = (int64_t)f[ERR_ROWS_OUTSIDE];
+    return PCT_OK;
+}
+
+static pct_status array_info(pct_ctx* c, pct_array which, void** p, size_t* bytes) {
+    const size_t V = (size_t)c->geo.num_voxels, B = (size_t)c->geo.num_bins, H = (size_t)c->h.n;
+    DevBuf* b = nullptr;
+    size_t n = 0;
+    switch (which) {
+        case PCT_ARR_MSC_COUNTS: b = &c->msc_counts; n = V * 4; break;
+        case PCT_ARR_SM_COUNTS: b = &c->sm_counts; n = V * 4; break;
+        case PCT_ARR_SC_HULL: b = &c->sc_hull; n = V * 4; break;
+        case PCT_ARR_MSC_HULL: b = &c->msc_hull; n = V * 4; break;
+        case PCT_ARR_SM_HULL: b = &c->sm_hull; n = V * 4; break;
+        case PCT_ARR_BIN_COUNTS_PRE: b = &c->bin_counts; n = B * 4; break;
+        case PCT_ARR_MEAN_WEPL: b = &c->mean_wepl; n = B * 4; break;
+        case PCT_ARR_MEAN_UT: b = &c->mean_ut; n = B * 4; break;
+        case PCT_ARR_MEAN_UV: b = &c->mean_uv; n = B * 4; break;
+        case PCT_ARR_SD_WEPL: b = &c->sd_wepl; n = B * 4; break;
+        case PCT_ARR_SD_UT: b = &c->sd_ut; n = B * 4; break;
+        case PCT_ARR_SD_UV: b = &c->sd_uv; n = B * 4; break;
+        case PCT_ARR_BIN_COUNTS_POST: b = &c->bin_counts_post; n = B * 4; break;
+        case PCT_ARR_SINOGRAM: b = &c->sinogram; n = B * 4; break;
+        case PCT_ARR_SINOGRAM_FILTERED: b = &c->sinogram_filtered; n = B * 4; break;
+        case PCT_ARR_FBP_IMAGE: b = &c->fbp_image; n = V * 4; break;
+        case PCT_ARR_FBP_HULL: b = &c->fbp_hull; n = V; break;
+        case PCT_ARR_X_HULL: b = &c->x_hull; n = V; break;
+        case PCT_ARR_X_HULL_FILTERED: b = &c->x_hull_filtered; n = V; break;
+        case PCT_ARR_X0: b = &c->x0; n = V * 4; break;
+        case PCT_ARR_X: b = &c->x; n = V * 4; break;
+        case PCT_ARR_H_BIN_NUM: b = &c->h.bin_num; n = H * 4; break;
+        case PCT_ARR_H_WEPL: b = &c->h.wepl; n = H * 4; break;
+        case PCT_ARR_H_X_ENTRY: b = &c->h.x_entry; n = H * 4; break;
+        case PCT_ARR_H_Y_ENTRY: b = &c->h.y_entry; n = H * 4; break;
+        case PCT_ARR_H_Z_ENTRY: b = &c->h.z_entry; n = H * 4; break;
+        case PCT_ARR_H_X_EXIT: b = &c->h.x_exit; n = H * 4; break;
+        case PCT_ARR_H_Y_EXIT: b = &c->h.y_exit; n = H * 4; break;
+        case PCT_ARR_H_Z_EXIT: b = &c->h.z_exit; n = H * 4; break;
+        case PCT_ARR_H_XY_ENTRY_ANGLE: b = &c->h.xy_entry_angle; n = H * 4; break;
+        case PCT_ARR_H_XZ_ENTRY_ANGLE: b = &c->h.xz_entry_angle; n = H * 4; break;
+        case PCT_ARR_H_XY_EXIT_ANGLE: b = &c->h.xy_exit_angle; n = H * 4; break;
+        case PCT_ARR_H_XZ_EXIT_ANGLE: b = &c->h.xz_exit_angle; n = H * 4; break;
+        case PCT_ARR_H_FIRST_VOXEL: b = &c->h.first_voxel; n = H * 4; break;
+        case PCT_ARR_H_FAILED_CUTS: b = &c->h.failed; n = H; break;
+        case PCT_ARR_ROW_OFFSETS: b = &c->row_offsets; n = c->stage >= ST_ROWS ? (H + 1) * 8 : 0; break;
+        case PCT_ARR_ROWS: b = &c->rows; n = c->stage >= ST_ROWS ? (size_t)c->counts.row_entries * 4 : 0; break;
+        case PCT_ARR_CHORD: b = &c->chord; n = c->stage >= ST_ROWS ? H * 4 : 0; break;
+        default: return pct_fail(PCT_ERR_ARGUMENT, "unknown array %d", (int)which);
+    }
+    if (n && (!b->p || b->bytes < n)) return pct_fail(PCT_ERR_STATE, "array %d is not available at this stage", (int)which);
+    *p = b->p;
+    *bytes = n;
+    return PCT_OK;
+}
+
+extern "C" pct_status pct_array_device_ptr(pct_ctx* c, pct_array which, void** dptr, size_t* bytes) {
+    if (!c || !dptr || !bytes) return pct_fail(PCT_ERR_ARGUMENT, "pct_array_device_ptr: null argument");
+    return array_info(c, which, dptr, bytes);
+}
+
+extern "C" pct_status pct_get_array(pct_ctx* c, pct_array which, void* host_dst, size_t* bytes) {
+    if (!c || !bytes) return pct_fail(PCT_ERR_ARGUMENT, "pct_get_array: null argument");
+    PCT_TRY(c->set_device());
+    void* p = nullptr;
+    size_t n = 0;
+    PCT_TRY(array_info(c, which, &p, &n));
+    if (!host_dst) {
+        *bytes = n;
+        return PCT_OK;
+    }
+    if (*bytes < n) return pct_fail(PCT_ERR_ARGUMENT, "pct_get_array: buffer holds %zu bytes, need %zu", *bytes, n);
+    if (n) {
+        PCT_CUDA(cudaMemcpyAsync(host_dst, p, n, cudaMemcpyDeviceToHost, c->stream));
+        PCT_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    *bytes = n;
+    return PCT_OK;
+}
+
+extern "C" pct_status pct_set_image(pct_ctx* c, const float* x) {
+    if (!c || !x) return pct_fail(PCT_ERR_ARGUMENT, "pct_set_image: null argument");
+    PCT_TRY(c->set_device());
+    size_t n = sizeof(float) * c->geo.num_voxels;
+    PCT_TRY(c->x.alloc(n));
+    PCT_TRY(c->x0.alloc(n));
+    PCT_CUDA(cudaMemcpyAsync(c->x.p, x, n, cudaMemcpyHostToDevice, c->stream));
+    PCT_CUDA(cudaMemcpyAsync(c->x0.p, x, n, cudaMemcpyHostToDevice, c->stream));
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    return PCT_OK;
+}
+
+/* ---- C ABI: stages ------------------------------------------------------------ */
+#define STAGE_ENTRY(c)                                                   \
+    if (!(c)) return pct_fail(PCT_ERR_ARGUMENT, "null context");         \
+    PCT_TRY((c)->set_device())
+
+extern "C" pct_status pct_process_chunk(pct_ctx* c, const float* const data13[13], const float* angle, int64_t n,
+                                        int on_dev) {
+    STAGE_ENTRY(c);
+    if (n < 0 || (n > 0 && (!data13 || !angle))) return pct_fail(PCT_ERR_ARGUMENT, "pct_process_chunk: bad arguments");
+    for (int k = 0; n > 0 && k < 13; ++k)
+        if (!data13[k]) return pct_fail(PCT_ERR_ARGUMENT, "pct_process_chunk: null array %d", k);
+    return pct_stage_process_chunk(c, data13, angle, n, on_dev);
+}
+extern "C" pct_status pct_hull_detection_finish(pct_ctx* c) { STAGE_ENTRY(c); return pct_stage_hull_finish(c); }
+extern "C" pct_status pct_statistical_cuts(pct_ctx* c) {
+    STAGE_ENTRY(c);
+    if (c->stage == ST_BINNED) PCT_TRY(pct_stage_hull_finish(c));
+    return pct_stage_cuts(c);
+}
+extern "C" pct_status pct_fbp(pct_ctx* c) {
+    STAGE_ENTRY(c);
+    if (!c->cfg.fbp_on) return PCT_OK;
+    return pct_stage_fbp(c);
+}
+extern "C" pct_status pct_hull_selection(pct_ctx* c) { STAGE_ENTRY(c); return pct_stage_hull_selection(c); }
+extern "C" pct_status pct_define_initial_iterate(pct_ctx* c) { STAGE_ENTRY(c); return pct_stage_initial_iterate(c); }
+extern "C" pct_status pct_collect_mlp_endpoints(pct_ctx* c) { STAGE_ENTRY(c); return pct_stage_endpoints(c); }
+extern "C" pct_status pct_mlp_rows(pct_ctx* c) { STAGE_ENTRY(c); return pct_stage_mlp_rows(c); }
+extern "C" pct_status pct_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
+    STAGE_ENTRY(c);
+    return pct_stage_drop(c, iterations, stats);
+}
+extern "C" pct_status pct_image_reconstruction(pct_ctx* c, pct_drop_stats* stats) {
+    STAGE_ENTRY(c);
+    PCT_TRY(pct_stage_endpoints(c));
+    PCT_TRY(pct_stage_mlp_rows(c));
+    return pct_stage_drop(c, c->cfg.iterations, stats);
+}

@@ -1,0 +1,151 @@
+/*
+ * Reconstruction context: configuration, stream and every device buffer of
+ * the path.  Internal to the library.
+ *
+ * Device data layout (all SoA, one CUDA allocation per array):
+ *   history store   capacity H: 10 float coordinates/angles, WEPL (float),
+ *                   bin (int32), flags (uint8), first voxel (uint32).  It is
+ *                   compacted in place after binning, cuts and endpoints,
+ *                   like the reference's *_vector globals.
+ *   bins            counts (int32), exact fixed-point sums (int64) and the
+ *                   binary32 means / sigmas / sinogram (NUM_BINS each).
+ *   voxels          hull count images (int32), hull masks (uint8), FBP
+ *                   image, iterate x, DROP update accumulator (float).
+ *   MLP rows        row offsets (int64, R+1), voxel entries (uint32), chord
+ *                   length (float) and 1/||a_i||^2 (double) per row; per-block
+ *                   diagonal weights for DROP.
+ */
+#ifndef PCT_CTX_H
+#define PCT_CTX_H
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include "pct_internal.h"
+
+#define PCT_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return pct_fail(PCT_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define PCT_TRY(call)                         \
+    do {                                      \
+        pct_status s_ = (call);               \
+        if (s_ != PCT_OK) return s_;          \
+    } while (0)
+
+/* Owning device buffer of bytes. */
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    pct_status alloc(size_t n);           /* reallocates when larger; contents lost */
+    pct_status grow_keep(size_t n, cudaStream_t s); /* reallocates keeping the old bytes */
+    void release();
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+/* Per-history arrays of the resident store. */
+struct HistoryStore {
+    DevBuf x_entry, y_entry, z_entry, x_exit, y_exit, z_exit;
+    DevBuf xy_entry_angle, xz_entry_angle, xy_exit_angle, xz_exit_angle;
+    DevBuf wepl, bin_num, bin_valid, failed, first_voxel;
+    int64_t n = 0, capacity = 0;
+    pct_status reserve(int64_t cap, cudaStream_t s);
+    void release();
+};
+
+/* Device-side view of the history store for kernels. */
+struct HistView {
+    float *x_entry, *y_entry, *z_entry, *x_exit, *y_exit, *z_exit;
+    float *xy_entry_angle, *xz_entry_angle, *xy_exit_angle, *xz_exit_angle;
+    float* wepl;
+    int32_t* bin_num;
+    uint8_t* bin_valid;
+    uint8_t* failed;
+    uint32_t* first_voxel;
+};
+
+/* Parameters every kernel needs (passed by value). */
+struct DevGeom {
+    int columns, rows, slices, num_voxels;
+    int t_bins, v_bins, angular_bins, num_bins;
+    double recon_cyl_radius, recon_cyl_height;
+    double voxel_width, voxel_height, voxel_thickness;
+    double x_zero, y_zero, z_zero, mlp_u_step;
+    double t_bin_size, v_bin_size, angular_bin_size, gantry_angle_interval, source_radius, slice_thickness;
+};
+
+enum Stage {
+    ST_EMPTY = 0, ST_BINNED, ST_HULLS_DONE, ST_CUT, ST_FBP, ST_HULL_SELECTED, ST_X0, ST_ENDPOINTS, ST_ROWS
+};
+
+struct pct_ctx {
+    pct_config cfg;
+    pct_geometry geo;
+    DevGeom dg;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int stage = ST_EMPTY;
+    pct_counts counts{};
+
+    /* chunk staging */
+    DevBuf in13[13], in_angle;
+    DevBuf tmp_missed, tmp_hist;   /* per-chunk flags and staging for compaction */
+    DevBuf scan_tmp;               /* block sums for stream compaction */
+    DevBuf pinned_count;           /* host-pinned counters read back after compactions */
+    HistoryStore h, h2;            /* h2: scratch store for out-of-place compaction */
+
+    /* bins */
+    DevBuf bin_counts, bin_counts_post, bin_sum1, bin_sum2, sino_sum;
+    DevBuf mean_wepl, mean_ut, mean_uv, sd_wepl, sd_ut, sd_uv, sinogram, sinogram_filtered;
+    DevBuf filter_taps, filter_scale, trig_gantry, trig_bins;
+    DevBuf err_flags;              /* device error/overflow counters */
+
+    /* voxels */
+    DevBuf sc_hull, msc_counts, sm_counts, msc_hull, sm_hull;
+    DevBuf fbp_image, fbp_hull, x_hull, x_hull_filtered, x0, x, x_update;
+
+    /* MLP rows and DROP */
+    DevBuf row_offsets, rows, chord, inv_norm, mlp_table;
+    DevBuf block_diag, block_diag_offsets;
+    DevBuf drop_resid;
+    cudaGraphExec_t drop_graph_exec = nullptr;  /* one DROP iteration */
+    int64_t row_capacity = 0;
+    int num_blocks = 0;
+    int diag_ready = 0;
+
+    pct_status set_device() {
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) return pct_fail(PCT_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+        return PCT_OK;
+    }
+    HistView view(HistoryStore& s) const;
+};
+
+/* Stage implementations (one file each). */
+pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], const float* angle, int64_t n, int on_dev);
+pct_status pct_stage_hull_finish(pct_ctx* c);
+pct_status pct_stage_cuts(pct_ctx* c);
+pct_status pct_stage_fbp(pct_ctx* c);
+pct_status pct_stage_hull_selection(pct_ctx* c);
+pct_status pct_stage_initial_iterate(pct_ctx* c);
+pct_status pct_stage_endpoints(pct_ctx* c);
+pct_status pct_stage_mlp_rows(pct_ctx* c);
+pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats);
+
+/* Stable compaction of src[src_off, src_off+n) by a keep flag into dst at dst_off. */
+pct_status pct_compact(pct_ctx* c, HistoryStore& src, int64_t src_off, int64_t n, const uint8_t* d_keep,
+                       HistoryStore& dst, int64_t dst_off, int64_t* kept);
+/* In-place stable compaction of the resident store c->h[0, n). */
+pct_status pct_compact_histories(pct_ctx* c, const uint8_t* d_keep, int64_t n, int64_t* kept);
+
+/* Device error counters (indices into err_flags, uint64). */
+enum { ERR_WALK_CAPPED = 0, ERR_VOXEL_OUTSIDE = 1, ERR_FIXED_OVERFLOW = 2, ERR_ROW_OVERFLOW = 3,
+       ERR_MLP_FP64 = 4, ERR_ROWS_OUTSIDE = 5, ERR_COUNT = 8 };
+
+DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g);
+void pct_drop_release_graph(pct_ctx* c);
+
+#endif

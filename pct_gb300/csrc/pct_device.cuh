@@ -1,0 +1,74 @@
+/*
+ * Device helpers shared by the kernels: voxel arithmetic of the reference
+ * walks and the exact fixed-point bin sums.
+ *
+ * The voxel helpers evaluate the reference's expressions
+ * (src/pCT_Reconstruction_Data_Segments.cu:8508-8752) in binary64 in source
+ * order; the library is compiled with -fmad=false, so no multiply-add pair
+ * is fused behind the source's back and the results equal the CPU oracle's.
+ */
+#ifndef PCT_DEVICE_CUH
+#define PCT_DEVICE_CUH
+
+#include <cstdint>
+#include "pct_ctx.h"
+
+#define PCT_X_INC 1    /* X_INCREASING_DIRECTION = RIGHT (pCT_data.h:275) */
+#define PCT_Y_INC (-1) /* DOWN */
+#define PCT_Z_INC (-1) /* DOWN */
+
+/* calculate_voxel_GPU (.cu:8508) */
+__device__ __forceinline__ int dev_calculate_voxel(double zero, double pos, double size) {
+    return pct_d2i(fabs(pos - zero) / size);
+}
+/* edge_coordinate_GPU (.cu:8735) */
+__device__ __forceinline__ double dev_edge_coordinate(double zero, int voxel_entered, double size, int inc, int step) {
+    int on_edge = (step == inc) ? voxel_entered : voxel_entered + 1;
+    return zero + (inc * on_edge * size);
+}
+/* distance_remaining_GPU (.cu:8721) */
+__device__ __forceinline__ double dev_distance_remaining(double zero, double pos, int inc, int step, double size,
+                                                         int voxel) {
+    return fabs(dev_edge_coordinate(zero, voxel + inc * step, size, inc, step) - pos);
+}
+/* corresponding_coordinate_GPU (.cu:8748) */
+__device__ __forceinline__ double dev_corresponding(double m, double x, double x0, double y0) {
+    return m * (x - x0) + y0;
+}
+
+/* Exact per-bin sums: binary32 summands in fixed point (2^32 for WEPL and
+ * squared WEPL deviations, 2^40 for angles, 2^48 for squared angle
+ * deviations); integer addition makes the sum independent of order. */
+#define PCT_SCALE_WEPL 4294967296.0
+#define PCT_SCALE_ANGLE 1099511627776.0
+#define PCT_SCALE_ANGLE_SQ 281474976710656.0
+
+__device__ __forceinline__ long long dev_to_fixed(float v, double scale) {
+    double s = (double)v * scale;
+    return (long long)(s >= 0 ? s + 0.5 : s - 0.5);
+}
+__device__ __forceinline__ void dev_add_fixed(long long* dst, long long v) {
+    atomicAdd((unsigned long long*)dst, (unsigned long long)v);
+}
+__host__ __device__ __forceinline__ float dev_from_fixed(long long s, double scale) {
+    return (float)((double)s / scale);
+}
+
+/* relative angle with the +-2 pi wrap (.cu:2557-2566) */
+__device__ __forceinline__ double dev_rel_angle(float exit_angle, float entry_angle) {
+    double r = exit_angle - entry_angle;
+    if (r > PCT_PI) r -= 2 * PCT_PI;
+    if (r < -PCT_PI) r += 2 * PCT_PI;
+    return r;
+}
+
+__device__ __forceinline__ void dev_flag(unsigned long long* flags, int which) {
+    atomicAdd(flags + which, 1ull);
+}
+
+static inline unsigned pct_grid_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    return (unsigned)(b > 0 ? b : 1);
+}
+
+#endif

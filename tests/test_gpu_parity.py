@@ -1,0 +1,155 @@
+"""CUDA path vs the CPU oracle, stage by stage (needs a GPU).
+
+Bit-exact: per-history intersections and bins, hull counts and hulls, bin
+means/sigmas (both sides use exact bin sums), cut masks, sinogram, filtered
+sinogram, FBP image, hull selection, initial iterate, MLP endpoints and MLP
+voxel rows.  DROP: the binary32 GPU iterate against the oracle's binary64 run
+of the same iterations, relative L2 <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+from pct_gb300 import phantoms, recon
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+DROP_TOL = 1e-4
+HIST_FIELDS = [("H_BIN_NUM", "bin_num"), ("H_WEPL", "WEPL"), ("H_X_ENTRY", "x_entry"), ("H_Y_ENTRY", "y_entry"),
+               ("H_Z_ENTRY", "z_entry"), ("H_X_EXIT", "x_exit"), ("H_Y_EXIT", "y_exit"), ("H_Z_EXIT", "z_exit"),
+               ("H_XY_ENTRY_ANGLE", "xy_entry_angle"), ("H_XZ_ENTRY_ANGLE", "xz_entry_angle"),
+               ("H_XY_EXIT_ANGLE", "xy_exit_angle"), ("H_XZ_EXIT_ANGLE", "xz_exit_angle")]
+
+CASES = {
+    "tiny_clip": lambda: (phantoms.tiny(num_histories=40000, seed=11, v_extent=0.55), {}),
+    "tiny_drop": lambda: (phantoms.tiny(num_histories=40000, seed=7, v_extent=0.3), {}),
+    "cfg1_sm": lambda: (phantoms.cfg1(num_histories=120000, seed=5), dict(iterations=2)),
+}
+
+
+def same(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return a.shape == b.shape and a.tobytes() == b.tobytes()
+
+
+def mismatch(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    if a.shape != b.shape:
+        return "shape %s vs %s" % (a.shape, b.shape)
+    d = np.nonzero(a.view(np.uint8).reshape(a.size, -1).any(axis=1) != 0)[0] if False else np.nonzero(a != b)[0]
+    return "%d of %d differ, first at %s: %s vs %s" % (len(d), a.size, d[:3], a[d[:3]], b[d[:3]])
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def run(request):
+    w, over = CASES[request.param]()
+    cfg_over = dict(w.config)
+    cfg_over.update(over)
+    cfg = phantoms.make_config(cfg_over)
+    data, angles = phantoms.generate(w)
+    ora = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_EXACT, keep_history=True)
+    r = recon.Reconstruction(cfg)
+    out = {}
+    # three chunks of unequal size: the resident store must come out as one batch would
+    n = data.shape[1]
+    cuts = [0, n // 3, n // 3 + n // 5, n]
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        r.process_chunk(data[:, a:b], angles[a:b])
+    out["binned"] = {k: r.array(k) for k, _ in HIST_FIELDS}
+    r.hull_detection_finish()
+    for k in ("MSC_COUNTS", "SM_COUNTS", "MSC_HULL", "SM_HULL"):
+        if (k.startswith("MSC") and cfg.msc_on) or (k.startswith("SM") and cfg.sm_on):
+            out[k] = r.array(k)
+    r.statistical_cuts()
+    for k in ("BIN_COUNTS_PRE", "MEAN_WEPL", "MEAN_UT", "MEAN_UV", "SD_WEPL", "SD_UT", "SD_UV", "BIN_COUNTS_POST",
+              "SINOGRAM"):
+        out[k] = r.array(k)
+    out["cut"] = {k: r.array(k) for k, _ in HIST_FIELDS}
+    r.FBP()
+    out["SINOGRAM_FILTERED"], out["FBP_IMAGE"], out["FBP_HULL"] = (r.array("SINOGRAM_FILTERED"), r.array("FBP_IMAGE"),
+                                                                   r.array("FBP_HULL"))
+    r.hull_selection()
+    out["X_HULL"], out["X_HULL_FILTERED"] = r.array("X_HULL"), r.array("X_HULL_FILTERED")
+    r.define_initial_iterate()
+    out["X0"] = r.array("X0")
+    r.collect_mlp_endpoints()
+    out["recon"] = {k: r.array(k) for k, _ in HIST_FIELDS}
+    out["recon"]["H_FIRST_VOXEL"] = r.array("H_FIRST_VOXEL")
+    r.mlp_rows()
+    out["ROW_OFFSETS"], out["ROWS"], out["CHORD"] = r.array("ROW_OFFSETS"), r.array("ROWS"), r.array("CHORD")
+    its = cfg.iterations
+    stats = r.drop(its)
+    out["X"] = r.array("X")
+    out["stats"] = stats
+    out["counts"] = r.counts()
+    r.close()
+    return request.param, cfg, ora, out
+
+
+def test_history_counts(run):
+    name, cfg, ora, out = run
+    c = out["counts"]
+    assert c["total_histories"] == int(ora["total_histories"][0])
+    assert c["recon_vol_histories"] == int(ora["recon_vol_histories"][0])
+    assert c["post_cut_histories"] == int(ora["post_cut_histories"][0])
+    assert c["reconstruction_histories"] == int(ora["reconstruction_histories"][0])
+    assert c["walks_capped"] == 0
+
+
+@pytest.mark.parametrize("stage", ["binned", "cut", "recon"])
+def test_history_store_bit_exact(run, stage):
+    name, cfg, ora, out = run
+    for k, f in HIST_FIELDS:
+        assert same(out[stage][k], ora[stage + "." + f]), "%s %s: %s" % (stage, k, mismatch(out[stage][k], ora[stage + "." + f]))
+    if stage == "recon":
+        assert same(out["recon"]["H_FIRST_VOXEL"], ora["recon.first_MLP_voxel"])
+
+
+def test_hulls_bit_exact(run):
+    name, cfg, ora, out = run
+    if cfg.msc_on:
+        assert same(out["MSC_COUNTS"], ora["MSC_counts_h"]), mismatch(out["MSC_COUNTS"], ora["MSC_counts_h"])
+        assert same(out["MSC_HULL"], ora["x_MSC"])
+    if cfg.sm_on:
+        assert same(out["SM_COUNTS"], ora["SM_counts_h"]), mismatch(out["SM_COUNTS"], ora["SM_counts_h"])
+        assert same(out["SM_HULL"], ora["x_SM"])
+    assert same(out["X_HULL"], ora["x_hull"])
+    assert same(out["X_HULL_FILTERED"], ora["x_hull_filtered"])
+
+
+def test_bin_statistics_and_sinogram_bit_exact(run):
+    name, cfg, ora, out = run
+    pairs = [("BIN_COUNTS_PRE", "bin_counts_h_pre"), ("MEAN_WEPL", "mean_WEPL_h"), ("MEAN_UT", "mean_rel_ut_angle_h"),
+             ("MEAN_UV", "mean_rel_uv_angle_h"), ("SD_WEPL", "stddev_WEPL_h"), ("SD_UT", "stddev_rel_ut_angle_h"),
+             ("SD_UV", "stddev_rel_uv_angle_h"), ("BIN_COUNTS_POST", "bin_counts_post"), ("SINOGRAM", "sinogram")]
+    for k, o in pairs:
+        assert same(out[k], ora[o]), "%s: %s" % (k, mismatch(out[k], ora[o]))
+
+
+def test_fbp_bit_exact(run):
+    name, cfg, ora, out = run
+    assert same(out["SINOGRAM_FILTERED"], ora["sinogram_filtered"]), mismatch(out["SINOGRAM_FILTERED"], ora["sinogram_filtered"])
+    assert same(out["FBP_IMAGE"], ora["FBP_image_h"]), mismatch(out["FBP_IMAGE"], ora["FBP_image_h"])
+    assert same(out["FBP_HULL"], ora["x_FBP"])
+    assert same(out["X0"], ora["x_k0"])
+
+
+def test_mlp_rows_bit_exact(run):
+    name, cfg, ora, out = run
+    offs, rows, chord = oracle.mlp_rows(cfg, ora["_hr"])
+    assert same(out["ROW_OFFSETS"], offs), mismatch(out["ROW_OFFSETS"], offs)
+    assert same(out["ROWS"], rows), mismatch(out["ROWS"], rows)
+    assert same(out["CHORD"], chord.astype(np.float32))
+
+
+def test_drop_within_tolerance_of_fp64(run):
+    name, cfg, ora, out = run
+    its = cfg.iterations
+    if its == 0:
+        pytest.skip("no iterations")
+    ref = ora["x_%d" % its]
+    err = np.linalg.norm(out["X"].astype(np.float64) - ref) / np.linalg.norm(ref)
+    assert err <= DROP_TOL, "relative L2 %.3e" % err
+    st = out["stats"]
+    assert st.iterations_run == its
+    assert all(np.isfinite(st.residual[k]) and st.residual[k] > 0 for k in range(its))
