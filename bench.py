@@ -1,0 +1,341 @@
+#!/usr/bin/env python3
+"""Benchmark: histories/s per MLP+DROP iteration on the production-size scan.
+
+Workload (the reference's production configuration on one GB300): a seeded
+synthetic scan of a 10 cm-radius water cylinder with 8 inserts (RSP 0.3-1.8),
+30M proton histories over 180 gantry angles, 256x256x32 voxels of
+1x1x2.5 mm, 12 DROP iterations with block size 200000 and lambda 0.1.  The
+synthetic generator stands in for the reference's PCTD scans (none ship).
+
+A step is one pass of the hot path over the resident histories: the MLP
+voxel rows of every recon history, then 12 DROP iterations (the iterate is
+reset to x0 first).  `value` = recon histories x 12 / step time, with the
+histories already in HBM.  `e2e` is the same metric for the whole
+reference-facing call sequence on a fresh context (pct_process_chunk from
+pinned host buffers through preprocessing, hulls, FBP, endpoints, MLP and
+DROP, then reading the image back), per step.
+
+  python bench.py [--steps K] [--warmup W] [--histories N] [--impl reference]
+
+With --impl reference the step is the reference algorithm on the CPU (the C
+restatement in oracle/, all host threads for the MLP rows and the DROP row
+updates) on a bounded sample of the same workload.
+Under torchrun (N > 1) every rank runs the same workload on its own GPU
+(replicas: the path has no cross-GPU exchange here) and `value` sums them.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "histories/s per MLP+DROP iteration"
+UNIT = "histories*iterations/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--histories", type=int, default=30_000_000)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-sample", type=int, default=6000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    def __init__(self, gpu):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.gpu = gpu
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q, "--format=csv,noheader",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+            self.f.close()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1].split()[0]))
+                    mx = max(mx, float(f[2].split()[0]))
+                except ValueError:
+                    continue
+                for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        except OSError:
+            pass
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def host_info():
+    cpu = "unknown"
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                cpu = line.split(":", 1)[1].strip()
+                break
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                cpu = line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return cpu, os.cpu_count()
+
+
+def cpu_baseline(cfg, r, sample, iterations, threads):
+    """The reference path (C restatement) on `sample` recon histories of the resident store."""
+    from oracle import oracle
+    keys = {"x_entry": "H_X_ENTRY", "y_entry": "H_Y_ENTRY", "z_entry": "H_Z_ENTRY", "x_exit": "H_X_EXIT",
+            "y_exit": "H_Y_EXIT", "z_exit": "H_Z_EXIT", "xy_entry_angle": "H_XY_ENTRY_ANGLE",
+            "xz_entry_angle": "H_XZ_ENTRY_ANGLE", "xy_exit_angle": "H_XY_EXIT_ANGLE", "xz_exit_angle": "H_XZ_EXIT_ANGLE",
+            "WEPL": "H_WEPL", "first_voxel": "H_FIRST_VOXEL"}
+    h = {k: r.array(v)[:sample].copy() for k, v in keys.items()}
+    x0 = r.array("X0").astype(np.float64)
+    return time_oracle(cfg, h, x0, iterations, threads)
+
+
+def time_oracle(cfg, h, x0, iterations, threads):
+    from oracle import oracle
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    n = len(h["WEPL"])
+    t0 = time.perf_counter()
+    offs, rows, chord = oracle.mlp_rows(cfg, h, threads=threads)
+    x = x0.copy()
+    x = oracle.drop(cfg, offs, rows, chord, h["WEPL"], x, iterations, cfg.block_size, float(np.float32(cfg.lambda_)),
+                    threads=threads)
+    dt = time.perf_counter() - t0
+    return n * iterations / dt, dt, n
+
+
+def run_reference_arm(a, ws, rank):
+    """--impl reference: the reference algorithm on the CPU, bounded sample per step."""
+    if rank != 0:
+        return
+    from pct_gb300 import phantoms
+    from oracle import oracle
+    w = phantoms.cfg2(num_histories=min(a.histories, 1_500_000))
+    cfg = phantoms.make_config(w.config)
+    data, angles = phantoms.generate(w)
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    ora = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_EXACT, iterations=0, keep_history=True)
+    hr = ora["_hr"]
+    sample = min(len(hr["WEPL"]), 40000)
+    h = {k: v[:sample].copy() for k, v in hr.items()}
+    x0 = ora["x_k0"].astype(np.float64)
+    for _ in range(a.warmup):
+        time_oracle(cfg, h, x0, cfg.iterations, threads)
+    times = []
+    for _ in range(a.steps):
+        v, dt, n = time_oracle(cfg, h, x0, cfg.iterations, threads)
+        times.append(dt)
+    value = sample * cfg.iterations * a.steps / sum(times)
+    cpu, ncores = host_info()
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": 1e3 * sum(times) / a.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded phantom generator, PCTD layout)",
+           "impl": "reference",
+           "config": {"workload": "cfg2 geometry 256x256x32, 12 DROP iterations, block 200000, lambda 0.1; "
+                                  "CPU sample of %d recon histories per step" % sample},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": "%d recon histories x %d iterations per step (MLP rows + DROP), %s"
+                                      % (sample, cfg.iterations, cpu)},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    a = parse()
+    ws, rank, local = dist_env()
+    if a.impl == "reference":
+        run_reference_arm(a, ws, rank)
+        return
+    import torch
+    from pct_gb300 import phantoms, recon
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    w = phantoms.cfg2(num_histories=a.histories, seed=2 + rank)
+    cfg = phantoms.make_config(w.config)
+    iters = cfg.iterations
+    data, angles = phantoms.generate(w)
+    n = data.shape[1]
+
+    # ---- setup: everything before the hot path, through the public API -------------
+    r = recon.Reconstruction(cfg, device=local)
+    r.reserve(n)
+    r.process_chunk(data, angles)
+    r.hull_detection_finish()
+    r.statistical_cuts()
+    r.FBP()
+    r.hull_selection()
+    r.define_initial_iterate()
+    r.collect_mlp_endpoints()
+    R = r.counts()["reconstruction_histories"]
+    stream = torch.cuda.ExternalStream(r.stream(), device=dev)
+
+    def step():
+        r.reset_iterate()
+        r.mlp_rows()
+        return r.drop(iters)
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    c0 = r.counts()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        drop_s = 0.0
+        for _ in range(a.steps):
+            st = step()
+            drop_s += st.seconds
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t = ev0.elapsed_time(ev1) * 1e-3
+    if dist:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    c1 = r.counts()
+    launches = c1["kernel_launches"] - c0["kernel_launches"]
+    rows = c1["row_entries"]
+    value = R * iters * a.steps / t * ws
+    mlp_s = t - drop_s
+    drop_iter_s = drop_s / (a.steps * iters)
+
+    # ---- roofline of the dominant kernel ----------------------------------------------
+    # DROP iteration: per row 8 B offset + 4 B chord + 8 B 1/||a||^2 + 4 B WEPL, 4 B per
+    # row entry read; image gathers/scatters stay in L2 and are not counted.
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    drop_bytes = R * 24 + rows * 4
+    mlp_bytes = R * 48 + rows * 4 + (R + 1) * 8 * 2
+    if drop_s >= mlp_s:
+        achieved = drop_bytes / drop_iter_s / 1e9
+        dom = "k_drop_rows (one DROP iteration)"
+    else:
+        achieved = mlp_bytes / (mlp_s / a.steps) / 1e9
+        dom = "k_mlp_count+k_mlp_fill (MLP rows)"
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
+        traffic = tr.get(dom.split()[0])
+    except Exception:
+        pass
+
+    # ---- end to end through the public API with host buffers --------------------------
+    pinned = torch.empty((13, n), dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = data
+    pang = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    pang.numpy()[:] = angles
+    e2e_t = 0.0
+    nv = phantoms.geometry(cfg).num_voxels
+    xhost = torch.empty(nv, dtype=torch.float32, pin_memory=True)
+    for _ in range(a.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q = recon.Reconstruction(cfg, device=local)
+        q.reserve(n)
+        q.process_chunk(pinned.numpy(), pang.numpy())
+        q.hull_detection_finish()
+        q.statistical_cuts()
+        q.FBP()
+        q.hull_selection()
+        q.define_initial_iterate()
+        q.image_reconstruction_GPU()
+        nb = C.c_size_t(nv * 4)
+        q._call("pct_get_array", recon.ARRAY_ID["X"], C.c_void_p(xhost.data_ptr()), C.byref(nb))
+        e2e_t += time.perf_counter() - t0
+        q.close()
+    e2e_value = R * iters * a.e2e_steps / e2e_t * ws
+
+    # ---- CPU baseline (rank 0, bounded sample) -------------------------------------------
+    cpu_b = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu, ncores = host_info()
+        v, dt, ns = cpu_baseline(cfg, r, a.cpu_sample, iters, 1)
+        cpu_b = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                 "sample": "%d recon histories x %d iterations (MLP rows + DROP) on 1 core of %s (%d cores), %.1f s"
+                           % (ns, iters, cpu, ncores, dt)}
+    r.close()
+    clocks = clk.summary()
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": t / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded phantom generator, PCTD layout)",
+            "config": {"workload": "cfg2: %d histories, %d recon histories, 180 angles, 256x256x32, %d DROP iterations,"
+                                   " block %d, lambda %.2g" % (n, R, iters, cfg.block_size, cfg.lambda_),
+                       "row_entries": rows, "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (MLP rows %.1f GB)" % (rows * 4 / 1e9),
+                       "mlp_ms_per_step": mlp_s / a.steps * 1e3, "drop_ms_per_iteration": drop_iter_s * 1e3},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * 14 * 4),
+                    "d2h_bytes_per_step": int(nv * 4), "seconds_per_step": e2e_t / a.e2e_steps},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"},
+            "cpu_baseline": cpu_b, "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

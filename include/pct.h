@@ -157,6 +157,7 @@ typedef struct pct_counts {
     int64_t rows_outside_image;      /* row entries whose voxel index lies outside the image */
     int64_t walks_capped;            /* hull/endpoint walks stopped by the step cap */
     int64_t mlp_fp64_samples;        /* MLP samples recomputed in FP64 near a voxel face */
+    int64_t kernel_launches;         /* kernels this context has launched (graph nodes included) */
 } pct_counts;
 
 /* Per-iteration DROP statistics (GB300 extension). */
@@ -212,7 +213,8 @@ pct_status pct_define_initial_iterate(pct_ctx* ctx);
 /* reconstruction_cuts (pCT_functions.h:230): hull entry/exit of each history,
  * compaction to the histories that cross the hull. */
 pct_status pct_collect_mlp_endpoints(pct_ctx* ctx);
-/* MLP voxel rows of every recon history, kept resident for all iterations. */
+/* MLP voxel rows of every recon history, kept resident for all iterations
+ * (may be called again to regenerate them). */
 pct_status pct_mlp_rows(pct_ctx* ctx);
 /* DROP iterations on the resident rows (the iteration loop of
  * image_reconstruction_GPU, src/pCT_Reconstruction_Data_Segments.cu:6795-6860).
@@ -227,6 +229,8 @@ pct_status pct_get_counts(pct_ctx* ctx, pct_counts* counts);
 pct_status pct_get_array(pct_ctx* ctx, pct_array which, void* host_dst, size_t* bytes);
 /* Device pointer and byte size of an array (valid until the next stage call). */
 pct_status pct_array_device_ptr(pct_ctx* ctx, pct_array which, void** dptr, size_t* bytes);
+/* Sets the current iterate back to the initial iterate x0. */
+pct_status pct_reset_iterate(pct_ctx* ctx);
 /* Replaces the current iterate (host pointer, num_voxels floats). */
 pct_status pct_set_image(pct_ctx* ctx, const float* x);
 /* CUDA stream the context runs on (cudaStream_t). */

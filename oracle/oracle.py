@@ -37,6 +37,9 @@ def load():
         _lib.ora_effective_chord_length.argtypes = [C.c_void_p, C.c_double, C.c_double]
         _lib.ora_drop.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.c_int, C.c_double, C.c_void_p]
+        _lib.ora_mlp_rows_mt.restype = C.c_int64
+        _lib.ora_drop_mt.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_int]
     return _lib
 
 
@@ -159,7 +162,7 @@ def endpoints(cfg, hull, h):
     return out
 
 
-def mlp_rows(cfg, h, capacity=None):
+def mlp_rows(cfg, h, capacity=None, threads=None):
     """h: recon vectors (x_entry.. are the hull entry/exit points). Returns (offsets, rows, chord)."""
     n = len(h["x_entry"])
     g = geometry(cfg)
@@ -168,20 +171,28 @@ def mlp_rows(cfg, h, capacity=None):
     offsets = np.empty(n + 1, np.int64)
     rows = np.empty(capacity, np.uint32)
     chord = np.empty(n, np.float64)
-    k = load().ora_mlp_rows(_cfgp(cfg), C.c_int64(n), *[_p(h[f]) for f in
-                                                         ("x_entry", "y_entry", "z_entry", "x_exit", "y_exit", "z_exit",
-                                                          "xy_entry_angle", "xz_entry_angle", "xy_exit_angle",
-                                                          "xz_exit_angle")],
-                            _p(h["first_voxel"]), _p(offsets), _p(rows), C.c_int64(capacity), _p(chord))
+    args = [_p(h[f]) for f in ("x_entry", "y_entry", "z_entry", "x_exit", "y_exit", "z_exit", "xy_entry_angle",
+                               "xz_entry_angle", "xy_exit_angle", "xz_exit_angle")]
+    if threads:
+        k = load().ora_mlp_rows_mt(_cfgp(cfg), C.c_int64(n), *args, _p(h["first_voxel"]), _p(offsets), _p(rows),
+                                   C.c_int64(capacity), _p(chord), C.c_int(threads))
+    else:
+        k = load().ora_mlp_rows(_cfgp(cfg), C.c_int64(n), *args, _p(h["first_voxel"]), _p(offsets), _p(rows),
+                                C.c_int64(capacity), _p(chord))
     if k < 0:
         raise RuntimeError("ora_mlp_rows: capacity too small")
     return offsets, rows[:k].copy(), chord
 
 
-def drop(cfg, offsets, rows, chord, wepl, x0, iterations, block_size, lam):
+def drop(cfg, offsets, rows, chord, wepl, x0, iterations, block_size, lam, threads=None):
     x = np.ascontiguousarray(x0, dtype=np.float64).copy()
-    rc = load().ora_drop(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord),
-                         _p(np.ascontiguousarray(wepl, np.float32)), iterations, block_size, C.c_double(lam), _p(x))
+    w = np.ascontiguousarray(wepl, np.float32)
+    if threads:
+        rc = load().ora_drop_mt(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord), _p(w),
+                                iterations, block_size, C.c_double(lam), _p(x), threads)
+    else:
+        rc = load().ora_drop(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord), _p(w), iterations,
+                             block_size, C.c_double(lam), _p(x))
     assert rc == 0
     return x
 

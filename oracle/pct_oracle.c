@@ -1000,3 +1000,98 @@ int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uin
     free(cnt);
     return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Multithreaded forms (same results) used to time the reference algorithm  */
+/* on all host cores.                                                         */
+/* ------------------------------------------------------------------------- */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int64_t ora_mlp_rows_mt(const pct_config* cfg, int64_t n, const float* x_in, const float* y_in, const float* z_in,
+                        const float* x_out, const float* y_out, const float* z_out, const float* xy_entry_angle,
+                        const float* xz_entry_angle, const float* xy_exit_angle, const float* xz_exit_angle,
+                        const uint32_t* first_voxel, int64_t* offsets, uint32_t* rows, int64_t capacity, double* chord,
+                        int threads) {
+    pct_geometry g;
+    if (pct_geometry_derive(cfg, &g)) return -1;
+    const int64_t maxlen = 8 * (g.columns + g.rows + g.slices) + 72;
+    int64_t* len = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    if (!len) return -1;
+    int failed = 0;
+#pragma omp parallel num_threads(threads)
+    {
+        uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)maxlen);
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t i = 0; i < n; ++i) {
+            double ae = xy_entry_angle[i], ax = xy_exit_angle[i], ze = xz_entry_angle[i], zx = xz_exit_angle[i];
+            chord[i] = ora_effective_chord_length(cfg, (ae + ax) / 2.0, (ze + zx) / 2.0);
+            int64_t k = tmp ? mlp_path(&g, x_in[i], y_in[i], z_in[i], x_out[i], y_out[i], z_out[i], ae, ze, ax, zx,
+                                       first_voxel[i], tmp, maxlen) : -1;
+            if (k < 0) failed = 1;
+            len[i] = k < 0 ? 0 : k;
+        }
+        free(tmp);
+    }
+    int64_t pos = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        offsets[i] = pos;
+        pos += len[i];
+    }
+    offsets[n] = pos;
+    free(len);
+    if (failed || pos > capacity) return -1;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        double ae = xy_entry_angle[i], ax = xy_exit_angle[i], ze = xz_entry_angle[i], zx = xz_exit_angle[i];
+        mlp_path(&g, x_in[i], y_in[i], z_in[i], x_out[i], y_out[i], z_out[i], ae, ze, ax, zx, first_voxel[i],
+                 rows + offsets[i], offsets[i + 1] - offsets[i]);
+    }
+    return pos;
+}
+
+int ora_drop_mt(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
+                const float* wepl, int iterations, int block_size, double lambda, double* x, int threads) {
+    pct_geometry g;
+    if (pct_geometry_derive(cfg, &g)) return 1;
+    const int nv = g.num_voxels;
+    double* upd = (double*)calloc((size_t)nv, sizeof(double));
+    uint32_t* cnt = (uint32_t*)calloc((size_t)nv, sizeof(uint32_t));
+    if (!upd || !cnt) { free(upd); free(cnt); return 2; }
+    for (int it = 0; it < iterations; ++it) {
+        for (int64_t start = 0; start < n; start += block_size) {
+            int64_t end = start + block_size < n ? start + block_size : n;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+            for (int64_t i = start; i < end; ++i) {
+                double c = chord[i];
+                int64_t a = offsets[i], b = offsets[i + 1];
+                double dot = 0.0;
+                for (int64_t j = a; j < b; ++j)
+                    if (rows[j] < (uint32_t)nv) dot += x[rows[j]];
+                dot *= c;
+                double aa = (c * c) * (double)(b - a);
+                double value = c * ((wepl[i] - dot) / aa) * lambda;
+                for (int64_t j = a; j < b; ++j) {
+                    uint32_t v = rows[j];
+                    if (v < (uint32_t)nv) {
+#pragma omp atomic update
+                        cnt[v] += 1;
+#pragma omp atomic update
+                        upd[v] += value;
+                    }
+                }
+            }
+#pragma omp parallel for num_threads(threads) schedule(static)
+            for (int v = 0; v < nv; ++v)
+                if (cnt[v] > 0) {
+                    x[v] += upd[v] / cnt[v];
+                    upd[v] = 0.0;
+                    cnt[v] = 0;
+                }
+        }
+    }
+    free(upd);
+    free(cnt);
+    return 0;
+}

@@ -89,6 +89,16 @@ double ora_effective_chord_length(const pct_config* cfg, double abs_angle_t, dou
 int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
              const float* wepl, int iterations, int block_size, double lambda, double* x);
 
+/* Same results with `threads` OpenMP threads (per-history parallel rows;
+ * per-block parallel DROP with atomic accumulation). */
+int64_t ora_mlp_rows_mt(const pct_config* cfg, int64_t n, const float* x_in, const float* y_in, const float* z_in,
+                        const float* x_out, const float* y_out, const float* z_out, const float* xy_entry_angle,
+                        const float* xz_entry_angle, const float* xy_exit_angle, const float* xz_exit_angle,
+                        const uint32_t* first_voxel, int64_t* offsets, uint32_t* rows, int64_t capacity, double* chord,
+                        int threads);
+int ora_drop_mt(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
+                const float* wepl, int iterations, int block_size, double lambda, double* x, int threads);
+
 /* Runtime of the library build (so callers can check they loaded the right one). */
 int ora_version(void);
 

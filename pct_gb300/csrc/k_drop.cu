@@ -114,6 +114,7 @@ static pct_status build_block_counts(pct_ctx* c) {
     PCT_CUDA(cudaMemsetAsync(c->block_diag.p, 0, sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
     for (int k = 0; k < nb; ++k) {
         int64_t s = k * B, e = s + B < n ? s + B : n;
+        ++c->launches;
         k_block_counts<<<1216, 256, 0, c->stream>>>(s, e, c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(),
                                                     (uint32_t)nv, c->block_diag.as<uint32_t>() + (size_t)k * nv);
     }
@@ -180,6 +181,8 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
     double res_host[maxit + 2];
     for (int it = 0; it < iterations; ++it) {
         PCT_CUDA(cudaGraphLaunch(c->drop_graph_exec, c->stream));
+        c->launches += 2 * (int64_t)c->num_blocks;
+        ++c->launches;
         k_store_resid<<<1, 1, 0, c->stream>>>(d_res + maxit, d_res + (it < maxit ? it : maxit - 1));
         ++done;
         if (c->cfg.residual_tol > 0.0) {

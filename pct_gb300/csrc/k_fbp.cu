@@ -157,26 +157,32 @@ pct_status pct_stage_fbp(pct_ctx* c) {
     const int T = c->geo.t_bins, A = c->geo.angular_bins, Vb = c->geo.v_bins, V = c->geo.num_voxels;
     PCT_TRY(c->filter_taps.alloc(sizeof(double) * (2 * T - 1)));
     PCT_TRY(c->filter_scale.alloc(sizeof(double) * T * Vb));
+    ++c->launches;
     k_filter_taps<<<pct_grid_for(2 * T - 1, 256), 256, 0, c->stream>>>(T, c->cfg.fbp_filter, c->cfg.t_bin_size,
                                                                        c->filter_taps.as<double>());
+    ++c->launches;
     k_filter_scale<<<pct_grid_for((int64_t)T * Vb, 256), 256, 0, c->stream>>>(
         T, Vb, c->cfg.t_bin_size, c->cfg.v_bin_size, c->cfg.source_radius, c->filter_scale.as<double>());
     size_t smem = sizeof(double) * T + sizeof(float) * T;
     if (smem > 48 * 1024) PCT_CUDA(cudaFuncSetAttribute(k_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int threads = T < 512 ? ((T + 31) / 32) * 32 : 512;
+    ++c->launches;
     k_filter<<<dim3(Vb, A), threads, smem, c->stream>>>(T, A, c->cfg.t_bin_size, c->sinogram.as<float>(),
                                                         c->filter_taps.as<double>(), c->filter_scale.as<double>(),
                                                         c->sinogram_filtered.as<float>());
     DevBuf trig;
     PCT_TRY(trig.alloc(sizeof(double2) * A));
+    ++c->launches;
     k_trig_bp<<<pct_grid_for(A, 256), 256, 0, c->stream>>>(A, c->cfg.gantry_angle_interval * PCT_ANGLE_TO_RADIANS,
                                                            trig.as<double2>());
     PCT_TRY(c->fbp_image.alloc(sizeof(float) * V));
     PCT_TRY(c->fbp_hull.alloc(V));
     size_t bsm = sizeof(double2) * A;
     if (bsm > 48 * 1024) PCT_CUDA(cudaFuncSetAttribute(k_backproject, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+    ++c->launches;
     k_backproject<<<pct_grid_for(V, 128), 128, bsm, c->stream>>>(c->dg, c->sinogram_filtered.as<float>(),
                                                                  trig.as<double2>(), c->fbp_image.as<float>());
+    ++c->launches;
     k_fbp_hull<<<pct_grid_for(V, 256), 256, 0, c->stream>>>(c->dg, c->cfg.fbp_threshold, c->fbp_image.as<float>(),
                                                             c->fbp_hull.as<uint8_t>());
     cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -199,6 +205,7 @@ pct_status pct_stage_initial_iterate(pct_ctx* c) {
         return pct_fail(PCT_ERR_STATE, "initial iterate needs the FBP image");
     PCT_TRY(c->x0.alloc(sizeof(float) * V));
     PCT_TRY(c->x.alloc(sizeof(float) * V));
+    ++c->launches;
     k_initial<<<pct_grid_for(V, 256), 256, 0, c->stream>>>(V, c->cfg.x_k0, c->fbp_image.as<float>(),
                                                            c->x_hull_filtered.as<uint8_t>(), c->x0.as<float>(),
                                                            c->x.as<float>());

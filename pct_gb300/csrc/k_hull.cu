@@ -256,14 +256,17 @@ static pct_status ensure_hull_images(pct_ctx* c) {
     unsigned grid = pct_grid_for(c->geo.num_voxels, 256);
     if (c->cfg.sc_on && !c->sc_hull.p) {
         PCT_TRY(c->sc_hull.alloc(V));
+        ++c->launches;
         k_init_hull<<<grid, 256, 0, c->stream>>>(c->dg, c->sc_hull.as<int>());
     }
     if (c->cfg.msc_on && !c->msc_counts.p) {
         PCT_TRY(c->msc_counts.alloc(V));
+        ++c->launches;
         k_init_hull<<<grid, 256, 0, c->stream>>>(c->dg, c->msc_counts.as<int>());
     }
     if (c->cfg.sm_on && !c->sm_counts.p) {
         PCT_TRY(c->sm_counts.alloc(V));
+        ++c->launches;
         k_init_hull<<<grid, 256, 0, c->stream>>>(c->dg, c->sm_counts.as<int>());
     }
     PCT_CUDA(cudaGetLastError());
@@ -276,12 +279,18 @@ pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed) {
     HistView h = c->view(c->h2);
     unsigned grid = pct_grid_for(n, 256);
     unsigned long long* flags = c->err_flags.as<unsigned long long>();
-    if (c->cfg.sc_on)
+    if (c->cfg.sc_on) {
+        ++c->launches;
         k_hull_walk<<<grid, 256, 0, c->stream>>>(c->dg, 0, c->cfg.sc_threshold, n, missed, h, c->sc_hull.as<int>(), flags);
-    if (c->cfg.msc_on)
+    }
+    if (c->cfg.msc_on) {
+        ++c->launches;
         k_hull_walk<<<grid, 256, 0, c->stream>>>(c->dg, 1, c->cfg.msc_threshold, n, missed, h, c->msc_counts.as<int>(), flags);
-    if (c->cfg.sm_on)
+    }
+    if (c->cfg.sm_on) {
+        ++c->launches;
         k_hull_walk<<<grid, 256, 0, c->stream>>>(c->dg, 2, c->cfg.sm_lower_threshold, n, missed, h, c->sm_counts.as<int>(), flags);
+    }
     PCT_CUDA(cudaGetLastError());
     return PCT_OK;
 }
@@ -293,6 +302,7 @@ pct_status pct_stage_hull_finish(pct_ctx* c) {
     unsigned grid = pct_grid_for(V, 256);
     if (c->cfg.msc_on) {
         PCT_TRY(c->msc_hull.alloc((size_t)V * 4));
+        ++c->launches;
         k_msc_edge<<<grid, 256, 0, c->stream>>>(c->dg, c->cfg.msc_diff_thresh, c->msc_counts.as<int>(),
                                                 c->msc_hull.as<int>());
     }
@@ -302,8 +312,11 @@ pct_status pct_stage_hull_finish(pct_ctx* c) {
         PCT_TRY(diff.alloc((size_t)V * 4 + (size_t)c->geo.slices * 4));
         int* d = diff.as<int>();
         int* thr = d + V;
+        ++c->launches;
         k_carve<<<grid, 256, 0, c->stream>>>(c->dg, c->sm_counts.as<int>(), d);
+        ++c->launches;
         k_sm_threshold<<<c->geo.slices, 1024, 0, c->stream>>>(c->dg, c->sm_counts.as<int>(), d, thr);
+        ++c->launches;
         k_sm_edge<<<grid, 256, 0, c->stream>>>(c->dg, c->cfg.sm_scale_threshold, c->sm_counts.as<int>(), thr,
                                                c->sm_hull.as<int>());
         cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -324,14 +337,17 @@ pct_status pct_stage_hull_selection(pct_ctx* c) {
     switch (c->cfg.mlp_hull) {
         case PCT_SC_HULL:
             if (!c->cfg.sc_on) return pct_fail(PCT_ERR_STATE, "MLP_HULL = SC_HULL needs sc_on");
+            ++c->launches;
             k_select_int<<<grid, 256, 0, c->stream>>>(V, c->sc_hull.as<int>(), c->x_hull.as<uint8_t>());
             break;
         case PCT_MSC_HULL:
             if (!c->cfg.msc_on) return pct_fail(PCT_ERR_STATE, "MLP_HULL = MSC_HULL needs msc_on");
+            ++c->launches;
             k_select_int<<<grid, 256, 0, c->stream>>>(V, c->msc_hull.as<int>(), c->x_hull.as<uint8_t>());
             break;
         case PCT_SM_HULL:
             if (!c->cfg.sm_on) return pct_fail(PCT_ERR_STATE, "MLP_HULL = SM_HULL needs sm_on");
+            ++c->launches;
             k_select_int<<<grid, 256, 0, c->stream>>>(V, c->sm_hull.as<int>(), c->x_hull.as<uint8_t>());
             break;
         default:
@@ -339,10 +355,11 @@ pct_status pct_stage_hull_selection(pct_ctx* c) {
             PCT_CUDA(cudaMemcpyAsync(c->x_hull.p, c->fbp_hull.p, V, cudaMemcpyDeviceToDevice, c->stream));
     }
     PCT_TRY(c->x_hull_filtered.alloc(V));
-    if (c->cfg.avg_filter_hull)
+    if (c->cfg.avg_filter_hull) {
+        ++c->launches;
         k_avg_filter<<<grid, 256, 0, c->stream>>>(c->dg, c->cfg.hull_filter_radius, c->cfg.hull_filter_threshold,
                                                   c->x_hull.as<uint8_t>(), c->x_hull_filtered.as<uint8_t>());
-    else
+    } else
         PCT_CUDA(cudaMemcpyAsync(c->x_hull_filtered.p, c->x_hull.p, V, cudaMemcpyDeviceToDevice, c->stream));
     PCT_CUDA(cudaGetLastError());
     c->stage = ST_HULL_SELECTED;

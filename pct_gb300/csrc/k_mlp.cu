@@ -328,38 +328,66 @@ __global__ void k_row_norms(DevGeom g, int64_t n, HistView h, const int64_t* __r
     inv_norm[i] = 1.0 / ((c * c) * nn);
 }
 
-/* Exclusive scan of int64 lengths into offsets[0..n] (single CTA, sequential tiles). */
-__global__ void k_scan64(const int64_t* __restrict__ len, int64_t n, int64_t* __restrict__ off) {
-    __shared__ int64_t carry;
+/* Exclusive scan of int64 lengths into offsets[0..n]: per-tile sums, a scan of
+ * the tile sums in one CTA, then a local scan per tile. */
+constexpr int SCAN_THREADS = 1024;
+
+__device__ __forceinline__ int64_t block_inclusive_scan(int64_t v, int64_t* ws) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int64_t s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        ws[lane] = s;
+    }
+    __syncthreads();
+    int64_t r = x + (w > 0 ? ws[w - 1] : 0);
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_tile_sum64(const int64_t* __restrict__ len, int64_t n, int64_t* __restrict__ tile_sum) {
     __shared__ int64_t ws[32];
+    int64_t i = (int64_t)blockIdx.x * SCAN_THREADS + threadIdx.x;
+    int64_t v = i < n ? len[i] : 0;
+    int64_t incl = block_inclusive_scan(v, ws);
+    if (threadIdx.x == SCAN_THREADS - 1) tile_sum[blockIdx.x] = incl;
+}
+
+__global__ void k_scan_tile_sums(int64_t* __restrict__ tile_sum, int64_t tiles, int64_t* __restrict__ total) {
+    __shared__ int64_t ws[32];
+    __shared__ int64_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int64_t base = 0; base < n; base += blockDim.x) {
+    for (int64_t base = 0; base < tiles; base += SCAN_THREADS) {
         int64_t i = base + threadIdx.x;
-        int64_t v = i < n ? len[i] : 0, x = v;
-        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        for (int o = 1; o < 32; o <<= 1) {
-            int64_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) ws[w] = x;
+        int64_t v = i < tiles ? tile_sum[i] : 0;
+        int64_t incl = block_inclusive_scan(v, ws);
+        if (i < tiles) tile_sum[i] = carry + incl - v;
         __syncthreads();
-        if (w == 0) {
-            int64_t s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int64_t y = __shfl_up_sync(0xffffffffu, s, o);
-                if (lane >= o) s += y;
-            }
-            ws[lane] = s;
-        }
-        __syncthreads();
-        int64_t incl = x + (w > 0 ? ws[w - 1] : 0);
-        if (i < n) off[i] = carry + incl - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        if (threadIdx.x == SCAN_THREADS - 1) carry += incl;
         __syncthreads();
     }
-    if (threadIdx.x == 0) off[n] = carry;
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_tile_scan64(const int64_t* __restrict__ len, int64_t n, const int64_t* __restrict__ tile_off,
+                              const int64_t* __restrict__ total, int64_t* __restrict__ off) {
+    __shared__ int64_t ws[32];
+    int64_t i = (int64_t)blockIdx.x * SCAN_THREADS + threadIdx.x;
+    int64_t v = i < n ? len[i] : 0;
+    int64_t incl = block_inclusive_scan(v, ws);
+    if (i < n) off[i] = tile_off[blockIdx.x] + incl - v;
+    if (i == 0) off[n] = *total;
 }
 
 }  // namespace
@@ -371,6 +399,7 @@ pct_status pct_stage_endpoints(pct_ctx* c) {
     uint8_t* keep = c->tmp_missed.as<uint8_t>();
     if (n > 0) {
         HistView h = c->view(c->h);
+        ++c->launches;
         k_endpoints<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, c->x_hull_filtered.as<uint8_t>(), h, keep,
                                                                  c->err_flags.as<unsigned long long>());
         PCT_CUDA(cudaGetLastError());
@@ -382,8 +411,27 @@ pct_status pct_stage_endpoints(pct_ctx* c) {
     return PCT_OK;
 }
 
+pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* off, int64_t* total) {
+    int64_t tiles = (n + SCAN_THREADS - 1) / SCAN_THREADS;
+    DevBuf tmp;
+    PCT_TRY(tmp.alloc(sizeof(int64_t) * (tiles + 1)));
+    int64_t* tile = tmp.as<int64_t>();
+    int64_t* d_total = tile + tiles;
+    ++c->launches;
+    k_tile_sum64<<<(unsigned)tiles, SCAN_THREADS, 0, c->stream>>>(len, n, tile);
+    ++c->launches;
+    k_scan_tile_sums<<<1, SCAN_THREADS, 0, c->stream>>>(tile, tiles, d_total);
+    ++c->launches;
+    k_tile_scan64<<<(unsigned)tiles, SCAN_THREADS, 0, c->stream>>>(len, n, tile, d_total, off);
+    PCT_CUDA(cudaMemcpyAsync(total, d_total, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    tmp.release();
+    if (e != cudaSuccess) return pct_fail(PCT_ERR_CUDA, "offset scan: %s", cudaGetErrorString(e));
+    return PCT_OK;
+}
+
 pct_status pct_stage_mlp_rows(pct_ctx* c) {
-    if (c->stage != ST_ENDPOINTS) return pct_fail(PCT_ERR_STATE, "mlp_rows needs collect_mlp_endpoints");
+    if (c->stage < ST_ENDPOINTS) return pct_fail(PCT_ERR_STATE, "mlp_rows needs collect_mlp_endpoints");
     const int64_t n = c->h.n;
     PCT_TRY(c->row_offsets.alloc(sizeof(int64_t) * (n + 1)));
     PCT_TRY(c->chord.alloc(sizeof(float) * (n > 0 ? n : 1)));
@@ -393,17 +441,17 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
     if (n > 0) {
         DevBuf len;
         PCT_TRY(len.alloc(sizeof(int64_t) * n));
+        ++c->launches;
         k_mlp_count<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, h, len.as<int64_t>());
-        k_scan64<<<1, 1024, 0, c->stream>>>(len.as<int64_t>(), n, c->row_offsets.as<int64_t>());
-        PCT_CUDA(cudaMemcpyAsync(&total, c->row_offsets.as<int64_t>() + n, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                 c->stream));
-        cudaError_t e = cudaStreamSynchronize(c->stream);
+        pct_status st = pct_scan_lengths(c, len.as<int64_t>(), n, c->row_offsets.as<int64_t>(), &total);
         len.release();
-        if (e != cudaSuccess) return pct_fail(PCT_ERR_CUDA, "MLP row count: %s", cudaGetErrorString(e));
+        PCT_TRY(st);
         PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (total > 0 ? total : 1)));
+        ++c->launches;
         k_mlp_fill<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, h, c->row_offsets.as<int64_t>(),
                                                                 c->rows.as<uint32_t>(),
                                                                 c->err_flags.as<unsigned long long>());
+        ++c->launches;
         k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_offsets.as<int64_t>(),
                                                                  c->chord.as<float>(), c->inv_norm.as<double>());
         PCT_CUDA(cudaGetLastError());

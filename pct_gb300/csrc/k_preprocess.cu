@@ -282,6 +282,7 @@ __global__ void k_invert(const uint8_t* __restrict__ a, uint8_t* __restrict__ b,
 }  // namespace
 
 static pct_status pct_invert_flags(pct_ctx* c, const uint8_t* a, uint8_t* b, int64_t n) {
+    ++c->launches;
     k_invert<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(a, b, n);
     PCT_CUDA(cudaGetLastError());
     return PCT_OK;
@@ -291,7 +292,9 @@ static pct_status ensure_tables(pct_ctx* c) {
     if (c->trig_gantry.p) return PCT_OK;
     PCT_TRY(c->trig_gantry.alloc(sizeof(double2) * 360));
     PCT_TRY(c->trig_bins.alloc(sizeof(double2) * c->geo.angular_bins));
+    ++c->launches;
     k_trig_table<<<2, 256, 0, c->stream>>>(c->trig_gantry.as<double2>(), 360, 1.0, PCT_ANGLE_TO_RADIANS);
+    ++c->launches;
     k_trig_table<<<pct_grid_for(c->geo.angular_bins, 256), 256, 0, c->stream>>>(
         c->trig_bins.as<double2>(), c->geo.angular_bins, c->cfg.angular_bin_size, PCT_ANGLE_TO_RADIANS);
     PCT_CUDA(cudaGetLastError());
@@ -342,6 +345,7 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
     uint8_t* missed = c->tmp_missed.as<uint8_t>();
     uint8_t* keep = missed + n;
     HistView stage = c->view(c->h2);
+    ++c->launches;
     k_preprocess<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(
         c->dg, in, d_angle, n, c->trig_gantry.as<double2>(), c->trig_bins.as<double2>(), stage, missed,
         c->bin_counts.as<int>(), c->bin_sum1.as<long long>(), 0);
@@ -367,13 +371,17 @@ pct_status pct_stage_cuts(pct_ctx* c) {
     const int nb = c->geo.num_bins;
     const int64_t n = c->h.n;
     HistView h = c->view(c->h);
+    ++c->launches;
     k_means<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts.as<int>(), c->bin_sum1.as<long long>(),
                                                           c->mean_wepl.as<float>(), c->mean_ut.as<float>(),
                                                           c->mean_uv.as<float>());
     PCT_CUDA(cudaMemsetAsync(c->bin_sum2.p, 0, (size_t)nb * 3 * 8, c->stream));
-    if (n > 0)
+    if (n > 0) {
+        ++c->launches;
         k_sq_dev<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, h, c->mean_wepl.as<float>(), c->mean_ut.as<float>(),
                                                                c->mean_uv.as<float>(), c->bin_sum2.as<long long>());
+    }
+    ++c->launches;
     k_sigma<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts.as<int>(), c->bin_sum2.as<long long>(),
                                                           c->cfg.sample_std_dev ? 1 : 0, c->sd_wepl.as<float>(),
                                                           c->sd_ut.as<float>(), c->sd_uv.as<float>());
@@ -381,11 +389,14 @@ pct_status pct_stage_cuts(pct_ctx* c) {
     PCT_CUDA(cudaMemsetAsync(c->sino_sum.p, 0, (size_t)nb * 8, c->stream));
     PCT_TRY(c->tmp_missed.alloc(n > 0 ? n : 1));
     uint8_t* keep = c->tmp_missed.as<uint8_t>();
-    if (n > 0)
+    if (n > 0) {
+        ++c->launches;
         k_cuts<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(
             n, h, c->cfg.sigmas_to_keep, c->mean_wepl.as<float>(), c->mean_ut.as<float>(), c->mean_uv.as<float>(),
             c->sd_wepl.as<float>(), c->sd_ut.as<float>(), c->sd_uv.as<float>(), keep, c->bin_counts_post.as<int>(),
             c->sino_sum.as<long long>());
+    }
+    ++c->launches;
     k_sinogram<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts_post.as<int>(),
                                                              c->sino_sum.as<long long>(), c->sinogram.as<float>());
     PCT_CUDA(cudaGetLastError());

@@ -203,7 +203,9 @@ pct_status pct_compact(pct_ctx* c, HistoryStore& src, int64_t src_off, int64_t n
     PCT_TRY(c->pinned_count.alloc(sizeof(int64_t) * 2));
     int64_t* d_total = c->pinned_count.as<int64_t>();
     PCT_TRY(dst.reserve(dst_off + n, c->stream));
+    ++c->launches;
     k_tile_counts<<<(unsigned)tiles, CT_THREADS, 0, c->stream>>>(d_keep, n, tile_counts);
+    ++c->launches;
     k_scan_tiles<<<1, 1024, 0, c->stream>>>(tile_counts, tile_offsets, (int)tiles, d_total);
     CompactArgs a;
     DevBuf* sf[] = {&src.x_entry, &src.y_entry, &src.z_entry, &src.x_exit, &src.y_exit, &src.z_exit,
@@ -219,6 +221,7 @@ pct_status pct_compact(pct_ctx* c, HistoryStore& src, int64_t src_off, int64_t n
         a.dst[q] = (char*)df[q]->p + dst_off * sz;
         a.size[q] = sz;
     }
+    ++c->launches;
     k_scatter<<<(unsigned)tiles, CT_THREADS, 0, c->stream>>>(d_keep, n, tile_offsets, a);
     PCT_CUDA(cudaGetLastError());
     int64_t total = 0;
@@ -311,6 +314,7 @@ extern "C" pct_status pct_get_counts(pct_ctx* c, pct_counts* out) {
     out->walks_capped = (int64_t)f[ERR_WALK_CAPPED];
     out->mlp_fp64_samples = (int64_t)f[ERR_MLP_FP64];
     out->rows_outside_image = (int64_t)f[ERR_ROWS_OUTSIDE];
+    out->kernel_launches = c->launches;
     return PCT_OK;
 }
 
@@ -438,4 +442,11 @@ extern "C" pct_status pct_image_reconstruction(pct_ctx* c, pct_drop_stats* stats
     PCT_TRY(pct_stage_endpoints(c));
     PCT_TRY(pct_stage_mlp_rows(c));
     return pct_stage_drop(c, c->cfg.iterations, stats);
+}
+
+extern "C" pct_status pct_reset_iterate(pct_ctx* c) {
+    STAGE_ENTRY(c);
+    if (!c->x0.p || !c->x.p) return pct_fail(PCT_ERR_STATE, "pct_reset_iterate: no initial iterate");
+    PCT_CUDA(cudaMemcpyAsync(c->x.p, c->x0.p, sizeof(float) * c->geo.num_voxels, cudaMemcpyDeviceToDevice, c->stream));
+    return PCT_OK;
 }

@@ -88,6 +88,7 @@ struct pct_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int stage = ST_EMPTY;
+    int64_t launches = 0;          /* kernels launched, for pct_counts.kernel_launches */
     pct_counts counts{};
 
     /* chunk staging */

@@ -30,7 +30,7 @@ class Counts(C.Structure):
     _fields_ = [("total_histories", C.c_int64), ("recon_vol_histories", C.c_int64),
                 ("post_cut_histories", C.c_int64), ("reconstruction_histories", C.c_int64),
                 ("row_entries", C.c_int64), ("rows_outside_image", C.c_int64), ("walks_capped", C.c_int64),
-                ("mlp_fp64_samples", C.c_int64)]
+                ("mlp_fp64_samples", C.c_int64), ("kernel_launches", C.c_int64)]
 
 
 class DropStats(C.Structure):
@@ -65,6 +65,7 @@ def _declare(lib):
     lib.pct_get_array.argtypes = [vp, ci, vp, C.POINTER(C.c_size_t)]
     lib.pct_array_device_ptr.argtypes = [vp, ci, C.POINTER(vp), C.POINTER(C.c_size_t)]
     lib.pct_set_image.argtypes = [vp, vp]
+    lib.pct_reset_iterate.argtypes = [vp]
     lib.pct_stream.restype = vp
     lib.pct_stream.argtypes = [vp]
 
@@ -147,6 +148,9 @@ class Reconstruction:
         st = DropStats()
         self._call("pct_image_reconstruction", C.byref(st))
         return st
+
+    def reset_iterate(self):
+        self._call("pct_reset_iterate")
 
     def set_image(self, x):
         x = np.ascontiguousarray(x, dtype=np.float32)
