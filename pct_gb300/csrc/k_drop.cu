@@ -23,17 +23,23 @@ namespace {
 constexpr int DROP_THREADS = 256;
 constexpr int DROP_WARPS = DROP_THREADS / 32;
 
-__global__ void k_block_counts(int64_t start, int64_t end, const int64_t* __restrict__ off,
-                               const uint32_t* __restrict__ rows, uint32_t nv, uint32_t* __restrict__ cnt) {
-    int64_t p0 = off[start], p1 = off[end];
-    for (int64_t p = p0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += (int64_t)gridDim.x * blockDim.x) {
+/* s_j of one block: one warp per row */
+__global__ void k_block_counts(int64_t start, int64_t end, const int64_t* __restrict__ row_start,
+                               const int* __restrict__ row_len, const uint32_t* __restrict__ rows, uint32_t nv,
+                               uint32_t* __restrict__ cnt) {
+    int lane = threadIdx.x & 31;
+    int64_t i = start + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    if (i >= end) return;
+    int64_t a = row_start[i], b = a + row_len[i];
+    for (int64_t p = a + lane; p < b; p += 32) {
         uint32_t v = rows[p];
         if (v < nv) atomicAdd(cnt + v, 1u);
     }
 }
 
 __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64_t end,
-                                                            const int64_t* __restrict__ off,
+                                                            const int64_t* __restrict__ row_start,
+                                                            const int* __restrict__ row_len,
                                                             const uint32_t* __restrict__ rows,
                                                             const float* __restrict__ chord,
                                                             const double* __restrict__ inv_norm,
@@ -45,7 +51,7 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
     int64_t i = start + (int64_t)blockIdx.x * DROP_WARPS + w;
     double r2 = 0.0;
     if (i < end) {
-        int64_t a = off[i], b = off[i + 1];
+        int64_t a = row_start[i], b = a + row_len[i];
         float dot = 0.0f;
         for (int64_t p = a + lane; p < b; p += 32) {
             uint32_t v = rows[p];
@@ -115,8 +121,9 @@ static pct_status build_block_counts(pct_ctx* c) {
     for (int k = 0; k < nb; ++k) {
         int64_t s = k * B, e = s + B < n ? s + B : n;
         ++c->launches;
-        k_block_counts<<<1216, 256, 0, c->stream>>>(s, e, c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(),
-                                                    (uint32_t)nv, c->block_diag.as<uint32_t>() + (size_t)k * nv);
+        k_block_counts<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
+            s, e, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), (uint32_t)nv,
+            c->block_diag.as<uint32_t>() + (size_t)k * nv);
     }
     PCT_CUDA(cudaGetLastError());
     c->num_blocks = nb;
@@ -132,7 +139,8 @@ static void enqueue_iteration(pct_ctx* c, double* resid) {
     for (int k = 0; k < c->num_blocks; ++k) {
         int64_t s = k * B, e = s + B < n ? s + B : n;
         unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
-        k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(),
+        k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+                                                          c->rows.as<uint32_t>(),
                                                           c->chord.as<float>(), c->inv_norm.as<double>(),
                                                           c->h.wepl.as<float>(), c->cfg.lambda, c->x.as<float>(),
                                                           c->x_update.as<float>(), (uint32_t)nv, resid);

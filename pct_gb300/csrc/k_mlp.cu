@@ -5,12 +5,15 @@
  *                 (.cu:5729-5770, 4997-5277): walk from the cylinder entry (and
  *                 backwards from the exit) to the first hull voxel; binary64 in
  *                 source order; bounded like the hull walks.
- *   k_mlp_count / k_mlp_fill
+ *   k_mlp_bound / k_mlp_fast
  *                 find_MLP_path_GPU (.cu:5279-5501): the Schulte most-likely path
  *                 sampled every MLP_U_STEP in depth, consecutive repeats dropped.
  *                 The rows are generated once and stay resident for every DROP
  *                 iteration (the reference recomputes them in every block of
- *                 every iteration).  Count pass, exclusive scan, fill pass.
+ *                 every iteration).  The sample count of a row is known from its
+ *                 depth u_2, so each row gets a slot of that size (k_mlp_bound +
+ *                 scan) and one pass fills it; binary32 samples with a binary64
+ *                 recomputation near voxel faces (see below).
  *   k_row_norms   EffectiveChordLength_GPU (.cu:4974-4995) per row and the DROP
  *                 row norm ||a_i||^2 = c^2 n (.cu:5825) kept as 1/||a_i||^2 in binary64.
  */
@@ -258,47 +261,192 @@ __device__ __forceinline__ int dev_mlp_voxel(const DevGeom& g, const MlpSetup& m
     return vx + vy * g.columns + vz * g.columns * g.rows;
 }
 
-/* Walks the MLP of history i; emit(voxel) is called for every row entry. */
-template <class Emit>
-__device__ __forceinline__ void dev_mlp_row(const DevGeom& g, const HistView& h, int64_t i, Emit emit) {
-    MlpSetup m;
-    dev_mlp_setup(h, i, m);
-    int prev = (int)h.first_voxel[i];
-    emit(prev);
-    const double STEP = g.mlp_u_step;
-    /* a path is never longer than the image diagonal; the cap only guards
-       against non-finite endpoints */
-    const int cap = 8 * (g.columns + g.rows + g.slices) + 64;
-    int k = 0;
-    for (double u_1 = STEP; u_1 < m.u_2 - STEP; u_1 += STEP) {
-        if (++k > cap) break;
-        int v = dev_mlp_voxel(g, m, u_1);
-        if ((uint32_t)v != (uint32_t)prev) {
-            emit(v);
-            prev = v;
+/* ---- binary32 fast path ------------------------------------------------------
+ * With s = u_2 - u the scattering moments of the exit side are polynomials in
+ * d = u_2 - u_1 with positive weights (no cancellation):
+ *   f(u_2 - s) = sum_m b_m s^m,  Q_j = sum_m b_m d^m / (m + j),
+ *   Sigma_2 = c_2 [[d^3 Q_3, d^2 Q_2], [d^2 Q_2, d Q_1]],
+ * and since the MLP of a straight line is the line,
+ *   t_1 = t_in + beta (t_out - t_in) + gamma (theta_out - theta_in),
+ * so binary32 only carries the deflection from the entry line.  The binary32
+ * result is within 4e-6 cm of the binary64 reference over 6.6e7 sampled MLP
+ * points; a sample whose x, y or z lies closer than mlp_face_margin to a voxel
+ * face is recomputed with the reference's binary64 expression
+ * (dev_mlp_voxel), so the voxel rows are those of the binary64 algorithm. */
+struct MlpTableEntry {
+    double u1;          /* u_1 after k steps of u_1 += MLP_U_STEP, as the reference accumulates it */
+    float u1_hi, u1_lo; /* u1 as a float pair */
+    float s1i0, s1i1, s1i3; /* Sigma_1^-1 at u_1 (binary64, rounded) */
+    float pad;
+};
+
+__global__ void k_mlp_u1(double step, int K, MlpTableEntry* __restrict__ tab) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double u = step;
+        for (int k = 0; k < K; ++k) {
+            tab[k].u1 = u;
+            u += step;
         }
     }
 }
 
-__global__ void __launch_bounds__(128) k_mlp_count(DevGeom g, int64_t n, HistView h, int64_t* __restrict__ len) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int64_t k = 0;
-    dev_mlp_row(g, h, i, [&](int) { ++k; });
-    len[i] = k;
+__global__ void k_mlp_table(int K, MlpTableEntry* __restrict__ tab) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    double u_1 = tab[k].u1;
+    double k1 = PCT_E_0 * (1 + 0.038 * pct_log(u_1 / PCT_X_0));
+    double c1 = k1 * k1 / PCT_X_0;
+    double st1 = c1 * (pct_cube(u_1) * (AL(0, 3) + u_1 * (AL(1, 12) + u_1 * (AL(2, 30) + u_1 * (AL(3, 60) + u_1 * (AL(4, 105) + AU(u_1, 5, 168)))))));
+    double stt1 = c1 * ((u_1 * u_1) * (AL(0, 2) + u_1 * (AL(1, 6) + u_1 * (AL(2, 12) + u_1 * (AL(3, 20) + u_1 * (AL(4, 30) + AU(u_1, 5, 42)))))));
+    double sth1 = c1 * (u_1 * (A0 + u_1 * (AL(1, 2) + u_1 * (AL(2, 3) + u_1 * (AL(3, 4) + u_1 * (AL(4, 5) + AU(u_1, 5, 6)))))));
+    double det1 = st1 * sth1 - stt1 * stt1;
+    tab[k].s1i0 = (float)(sth1 / det1);
+    tab[k].s1i1 = (float)(-stt1 / det1);
+    tab[k].s1i3 = (float)(st1 / det1);
+    float hi = (float)u_1;
+    tab[k].u1_hi = hi;
+    tab[k].u1_lo = (float)(u_1 - (double)hi);
+    tab[k].pad = 0.0f;
 }
 
-__global__ void __launch_bounds__(128) k_mlp_fill(DevGeom g, int64_t n, HistView h, const int64_t* __restrict__ off,
-                                                  uint32_t* __restrict__ rows, unsigned long long* __restrict__ flags) {
+/* Samples of history i: u_1 = tab[k].u1 for k < K with u_1 < u_2 - step (.cu:5376). */
+__device__ __forceinline__ int dev_sample_count(const MlpTableEntry* __restrict__ tab, int kmax, double u_2, double step) {
+    double lim = u_2 - step;
+    int lo = 0, hi = kmax; /* first k with u1 >= lim */
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (tab[mid].u1 < lim) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_mlp_bound(DevGeom g, int64_t n, HistView h,
+                                                   const MlpTableEntry* __restrict__ tab, int kmax,
+                                                   int64_t* __restrict__ bound) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int64_t p = off[i], end = off[i + 1];
-    int outside = 0;
-    dev_mlp_row(g, h, i, [&](int v) {
-        if (p < end) rows[p++] = (uint32_t)v;
-        if ((uint32_t)v >= (uint32_t)g.num_voxels) ++outside;
-    });
+    MlpSetup m;
+    dev_mlp_setup(h, i, m);
+    bound[i] = (int64_t)dev_sample_count(tab, kmax, m.u_2, g.mlp_u_step) + 1;
+}
+
+__device__ __forceinline__ float face_distance(float pos, float zero, float size, float inv_size) {
+    float q = fabsf(pos - zero) * inv_size;
+    float fr = q - floorf(q);
+    return fminf(fr, 1.0f - fr) * size;
+}
+
+__global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, HistView h,
+                                                  const MlpTableEntry* __restrict__ tab, int kmax, float margin,
+                                                  const int64_t* __restrict__ row_start, uint32_t* __restrict__ rows,
+                                                  int* __restrict__ row_len, unsigned long long* __restrict__ flags) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    MlpSetup m;
+    dev_mlp_setup(h, i, m);
+    const int K = dev_sample_count(tab, kmax, m.u_2, g.mlp_u_step);
+    /* Taylor coefficients of the scattering power around u_2 (binary64, then float) */
+    const double A[6] = {A0, PCT_A1_M * PCT_A1_P, PCT_A2_M * PCT_A2_P, PCT_A3_M * PCT_A3_P, PCT_A4_M * PCT_A4_P,
+                         PCT_A5_M * PCT_A5_P};
+    float b[6];
+#pragma unroll
+    for (int mm = 0; mm < 6; ++mm) {
+        double sum = 0.0, up = 1.0, binom = 1.0;
+        for (int k = mm; k < 6; ++k) {
+            sum += binom * A[k] * up;
+            up *= m.u_2;
+            binom = binom * (k + 1) / (k + 1 - mm);
+        }
+        b[mm] = (float)((mm & 1) ? -sum : sum);
+    }
+    const float u2_hi = (float)m.u_2, u2_lo = (float)(m.u_2 - (double)u2_hi);
+    const float dT = (float)(m.T20 - m.T0), dV = (float)(m.V20 - m.V0);
+    const float T21 = (float)m.T21, V21 = (float)m.V21;
+    const float cef = (float)m.ce, sef = (float)m.se;
+    const float x_in = h.x_entry[i], y_in = h.y_entry[i], V0 = (float)m.V0;
+    /* x at depth u_1 on the entry line: x_in + ce u_1 (the entry point has depth 0) */
+    const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
+    const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
+    const float iVW = 1.0f / VW, iVH = 1.0f / VH, iVT = 1.0f / VT;
+    const float lnX0 = __logf(36.08f);
+    int64_t out = row_start[i];
+    int len = 0;
+    uint32_t prev = h.first_voxel[i];
+    rows[out + len++] = prev;
+    int exact_samples = 0, outside = prev >= (uint32_t)g.num_voxels;
+    for (int k = 0; k < K; ++k) {
+        const MlpTableEntry te = tab[k];
+        float d = (u2_hi - te.u1_hi) + (u2_lo - te.u1_lo);
+        float k2 = 13.6f * (1.0f + 0.038f * (__logf(d) - lnX0));
+        float c2 = k2 * k2 * (1.0f / 36.08f);
+        float Q1 = b[5] * (1.0f / 6), Q2 = b[5] * (1.0f / 7), Q3 = b[5] * (1.0f / 8);
+        Q1 = fmaf(Q1, d, b[4] * (1.0f / 5)); Q2 = fmaf(Q2, d, b[4] * (1.0f / 6)); Q3 = fmaf(Q3, d, b[4] * (1.0f / 7));
+        Q1 = fmaf(Q1, d, b[3] * (1.0f / 4)); Q2 = fmaf(Q2, d, b[3] * (1.0f / 5)); Q3 = fmaf(Q3, d, b[3] * (1.0f / 6));
+        Q1 = fmaf(Q1, d, b[2] * (1.0f / 3)); Q2 = fmaf(Q2, d, b[2] * (1.0f / 4)); Q3 = fmaf(Q3, d, b[2] * (1.0f / 5));
+        Q1 = fmaf(Q1, d, b[1] * (1.0f / 2)); Q2 = fmaf(Q2, d, b[1] * (1.0f / 3)); Q3 = fmaf(Q3, d, b[1] * (1.0f / 4));
+        Q1 = fmaf(Q1, d, b[0]);              Q2 = fmaf(Q2, d, b[0] * (1.0f / 2)); Q3 = fmaf(Q3, d, b[0] * (1.0f / 3));
+        /* E1 = Q1 - Q2 (weights 1/((m+1)(m+2))), E2 = Q1 - 2 Q2 + Q3, E3 = Q2 - Q3, each summed directly */
+        float E1 = b[5] * (1.0f / 42), E2 = b[5] * (2.0f / 336), E3 = b[5] * (1.0f / 56);
+        E1 = fmaf(E1, d, b[4] * (1.0f / 30)); E2 = fmaf(E2, d, b[4] * (2.0f / 210)); E3 = fmaf(E3, d, b[4] * (1.0f / 42));
+        E1 = fmaf(E1, d, b[3] * (1.0f / 20)); E2 = fmaf(E2, d, b[3] * (2.0f / 120)); E3 = fmaf(E3, d, b[3] * (1.0f / 30));
+        E1 = fmaf(E1, d, b[2] * (1.0f / 12)); E2 = fmaf(E2, d, b[2] * (2.0f / 60));  E3 = fmaf(E3, d, b[2] * (1.0f / 20));
+        E1 = fmaf(E1, d, b[1] * (1.0f / 6));  E2 = fmaf(E2, d, b[1] * (2.0f / 24));  E3 = fmaf(E3, d, b[1] * (1.0f / 12));
+        E1 = fmaf(E1, d, b[0] * (1.0f / 2));  E2 = fmaf(E2, d, b[0] * (2.0f / 6));   E3 = fmaf(E3, d, b[0] * (1.0f / 6));
+        float D = fmaf(Q3, Q1, -Q2 * Q2);
+        float inv = 1.0f / (c2 * D);
+        float id = 1.0f / d;
+        float id2 = id * id, id3 = id2 * id;
+        float Aa = Q1 * inv * id3;      /* (Sigma_2^-1)_00 */
+        float Bm = E1 * inv * id2;      /* (R1^T Sigma_2^-1 R1)_01 */
+        float Cm = E2 * inv * id;       /* (R1^T Sigma_2^-1 R1)_11 */
+        float bb = -Q2 * inv * id2;     /* (Sigma_2^-1)_01 */
+        float e3 = -E3 * inv * id;      /* d (Sigma_2^-1)_01 + (Sigma_2^-1)_11 */
+        float ft0 = te.s1i0 + Aa, ft1 = te.s1i1 + Bm, ft3 = te.s1i3 + Cm;
+        float idet = 1.0f / fmaf(ft0, ft3, -ft1 * ft1);
+        float beta = fmaf(ft3, Aa, -ft1 * Bm) * idet;
+        float gam = fmaf(ft3, bb, -ft1 * e3) * idet;
+        float ct = fmaf(beta, dT, gam * T21);
+        float cv = fmaf(beta, dV, gam * V21);
+        float u1f = te.u1_hi;
+        float x1 = x_in + fmaf(cef, u1f, -sef * ct);
+        float y1 = y_in + fmaf(sef, u1f, cef * ct);
+        float z1 = V0 + cv;
+        uint32_t v;
+        if (face_distance(x1, X0, VW, iVW) < margin || face_distance(y1, Y0, VH, iVH) < margin ||
+            face_distance(z1, Z0, VT, iVT) < margin || !(fabsf(ct) < 1e3f) || !(fabsf(cv) < 1e3f)) {
+            v = (uint32_t)dev_mlp_voxel(g, m, te.u1);
+            ++exact_samples;
+        } else {
+            int vx = (int)(fabsf(x1 - X0) * iVW);
+            int vy = (int)(fabsf(y1 - Y0) * iVH);
+            int vz = (int)(fabsf(z1 - Z0) * iVT);
+            v = (uint32_t)(vx + vy * g.columns + vz * g.columns * g.rows);
+        }
+        if (v != prev) {
+            rows[out + len++] = v;
+            prev = v;
+            outside += v >= (uint32_t)g.num_voxels;
+        }
+    }
+    row_len[i] = len;
+    if (exact_samples) atomicAdd(flags + ERR_MLP_FP64, (unsigned long long)exact_samples);
     if (outside) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
+}
+
+/* Dense copy of the bounded rows (for pct_get_array). */
+__global__ void k_pack_rows(int64_t n, const int64_t* __restrict__ start, const int* __restrict__ len,
+                            const int64_t* __restrict__ dense_off, const uint32_t* __restrict__ rows,
+                            uint32_t* __restrict__ dense) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t s = start[i], d = dense_off[i];
+    for (int j = 0; j < len[i]; ++j) dense[d + j] = rows[s + j];
+}
+
+__global__ void k_len64(int64_t n, const int* __restrict__ len, int64_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = len[i];
 }
 
 /* EffectiveChordLength_GPU (.cu:4974-4995) with correctly rounded sinf/cosf */
@@ -317,14 +465,14 @@ __device__ double dev_chord(const DevGeom& g, double abs_angle_t, double abs_ang
     return VW * c2d * c3d;
 }
 
-__global__ void k_row_norms(DevGeom g, int64_t n, HistView h, const int64_t* __restrict__ off, float* __restrict__ chord,
+__global__ void k_row_norms(DevGeom g, int64_t n, HistView h, const int* __restrict__ len, float* __restrict__ chord,
                             double* __restrict__ inv_norm) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double ae = h.xy_entry_angle[i], ax = h.xy_exit_angle[i], ze = h.xz_entry_angle[i], zx = h.xz_exit_angle[i];
     double c = dev_chord(g, (ae + ax) / 2.0, (ze + zx) / 2.0);
     chord[i] = (float)c;
-    double nn = (double)(off[i + 1] - off[i]);
+    double nn = (double)len[i];
     inv_norm[i] = 1.0 / ((c * c) * nn);
 }
 
@@ -430,37 +578,83 @@ pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* 
     return PCT_OK;
 }
 
+static pct_status ensure_mlp_table(pct_ctx* c, int* kmax) {
+    const int K = 8 * (c->geo.columns + c->geo.rows + c->geo.slices) + 64;
+    *kmax = K;
+    if (c->mlp_table.p) return PCT_OK;
+    PCT_TRY(c->mlp_table.alloc(sizeof(MlpTableEntry) * K));
+    MlpTableEntry* tab = c->mlp_table.as<MlpTableEntry>();
+    ++c->launches;
+    k_mlp_u1<<<1, 1, 0, c->stream>>>(c->geo.mlp_u_step, K, tab);
+    ++c->launches;
+    k_mlp_table<<<pct_grid_for(K, 128), 128, 0, c->stream>>>(K, tab);
+    PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
+
 pct_status pct_stage_mlp_rows(pct_ctx* c) {
     if (c->stage < ST_ENDPOINTS) return pct_fail(PCT_ERR_STATE, "mlp_rows needs collect_mlp_endpoints");
     const int64_t n = c->h.n;
     PCT_TRY(c->row_offsets.alloc(sizeof(int64_t) * (n + 1)));
+    PCT_TRY(c->row_len.alloc(sizeof(int) * (n > 0 ? n : 1)));
     PCT_TRY(c->chord.alloc(sizeof(float) * (n > 0 ? n : 1)));
     PCT_TRY(c->inv_norm.alloc(sizeof(double) * (n > 0 ? n : 1)));
-    int64_t total = 0;
+    int kmax = 0;
+    PCT_TRY(ensure_mlp_table(c, &kmax));
+    int64_t bound_total = 0;
     HistView h = c->view(c->h);
+    unsigned long long* flags = c->err_flags.as<unsigned long long>();
     if (n > 0) {
-        DevBuf len;
-        PCT_TRY(len.alloc(sizeof(int64_t) * n));
+        DevBuf bound;
+        PCT_TRY(bound.alloc(sizeof(int64_t) * n));
         ++c->launches;
-        k_mlp_count<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, h, len.as<int64_t>());
-        pct_status st = pct_scan_lengths(c, len.as<int64_t>(), n, c->row_offsets.as<int64_t>(), &total);
-        len.release();
+        k_mlp_bound<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->mlp_table.as<MlpTableEntry>(), kmax,
+                                                                 bound.as<int64_t>());
+        pct_status st = pct_scan_lengths(c, bound.as<int64_t>(), n, c->row_offsets.as<int64_t>(), &bound_total);
+        c->launches += 3;
+        bound.release();
         PCT_TRY(st);
-        PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (total > 0 ? total : 1)));
+        PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (bound_total > 0 ? bound_total : 1)));
+        float margin = c->cfg.mlp_exact ? 3.0e38f : (float)c->cfg.mlp_face_margin;
         ++c->launches;
-        k_mlp_fill<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, h, c->row_offsets.as<int64_t>(),
-                                                                c->rows.as<uint32_t>(),
-                                                                c->err_flags.as<unsigned long long>());
+        k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, h, c->mlp_table.as<MlpTableEntry>(), kmax,
+                                                                margin, c->row_offsets.as<int64_t>(),
+                                                                c->rows.as<uint32_t>(), c->row_len.as<int>(), flags);
         ++c->launches;
-        k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_offsets.as<int64_t>(),
+        k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(),
                                                                  c->chord.as<float>(), c->inv_norm.as<double>());
         PCT_CUDA(cudaGetLastError());
-    } else {
-        PCT_CUDA(cudaMemsetAsync(c->row_offsets.p, 0, sizeof(int64_t), c->stream));
     }
-    c->counts.row_entries = total;
+    c->row_capacity = bound_total;
+    c->counts.row_entries = -1; /* computed on demand */
     c->diag_ready = 0;
     pct_drop_release_graph(c);
     c->stage = ST_ROWS;
     return PCT_OK;
 }
+
+/* Number of row entries, dense offsets (n+1) and, if dense != NULL, the dense rows. */
+pct_status pct_rows_dense(pct_ctx* c, int64_t* total, DevBuf* dense_off, DevBuf* dense) {
+    const int64_t n = c->h.n;
+    PCT_TRY(dense_off->alloc(sizeof(int64_t) * (n + 1)));
+    if (n == 0) {
+        *total = 0;
+        PCT_CUDA(cudaMemsetAsync(dense_off->p, 0, sizeof(int64_t), c->stream));
+        return PCT_OK;
+    }
+    DevBuf len64;
+    PCT_TRY(len64.alloc(sizeof(int64_t) * n));
+    k_len64<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->row_len.as<int>(), len64.as<int64_t>());
+    pct_status st = pct_scan_lengths(c, len64.as<int64_t>(), n, dense_off->as<int64_t>(), total);
+    len64.release();
+    PCT_TRY(st);
+    if (dense) {
+        PCT_TRY(dense->alloc(sizeof(uint32_t) * (*total > 0 ? *total : 1)));
+        k_pack_rows<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+                                                                 dense_off->as<int64_t>(), c->rows.as<uint32_t>(),
+                                                                 dense->as<uint32_t>());
+        PCT_CUDA(cudaGetLastError());
+    }
+    return PCT_OK;
+}
+

@@ -278,7 +278,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
     if (!c) return PCT_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf* all[] = {&c->in_angle, &c->tmp_missed, &c->tmp_hist, &c->scan_tmp, &c->pinned_count, &c->bin_counts,
+    DevBuf* all[] = {&c->dense_off, &c->dense_rows, &c->row_len, &c->in_angle, &c->tmp_missed, &c->tmp_hist, &c->scan_tmp, &c->pinned_count, &c->bin_counts,
                      &c->bin_counts_post, &c->bin_sum1, &c->bin_sum2, &c->sino_sum, &c->mean_wepl, &c->mean_ut,
                      &c->mean_uv, &c->sd_wepl, &c->sd_ut, &c->sd_uv, &c->sinogram, &c->sinogram_filtered,
                      &c->filter_taps, &c->filter_scale, &c->trig_gantry, &c->trig_bins, &c->err_flags,
@@ -311,6 +311,14 @@ extern "C" pct_status pct_get_counts(pct_ctx* c, pct_counts* out) {
     PCT_CUDA(cudaMemcpyAsync(f, c->err_flags.p, sizeof(f), cudaMemcpyDeviceToHost, c->stream));
     PCT_CUDA(cudaStreamSynchronize(c->stream));
     *out = c->counts;
+    if (c->stage >= ST_ROWS) {
+        DevBuf off;
+        int64_t total = 0;
+        pct_status st = pct_rows_dense(c, &total, &off, nullptr);
+        off.release();
+        PCT_TRY(st);
+        out->row_entries = total;
+    }
     out->walks_capped = (int64_t)f[ERR_WALK_CAPPED];
     out->mlp_fp64_samples = (int64_t)f[ERR_MLP_FP64];
     out->rows_outside_image = (int64_t)f[ERR_ROWS_OUTSIDE];
@@ -319,6 +327,11 @@ extern "C" pct_status pct_get_counts(pct_ctx* c, pct_counts* out) {
 }
 
 static pct_status array_info(pct_ctx* c, pct_array which, void** p, size_t* bytes) {
+    if ((which == PCT_ARR_ROW_OFFSETS || which == PCT_ARR_ROWS) && c->stage >= ST_ROWS) {
+        /* rows live in per-row slots; these arrays are the dense (CSR) view */
+        PCT_TRY(pct_rows_dense(c, &c->dense_total, &c->dense_off, which == PCT_ARR_ROWS ? &c->dense_rows : nullptr));
+        PCT_CUDA(cudaStreamSynchronize(c->stream));
+    }
     const size_t V = (size_t)c->geo.num_voxels, B = (size_t)c->geo.num_bins, H = (size_t)c->h.n;
     DevBuf* b = nullptr;
     size_t n = 0;
@@ -358,8 +371,8 @@ static pct_status array_info(pct_ctx* c, pct_array which, void** p, size_t* byte
         case PCT_ARR_H_XZ_EXIT_ANGLE: b = &c->h.xz_exit_angle; n = H * 4; break;
         case PCT_ARR_H_FIRST_VOXEL: b = &c->h.first_voxel; n = H * 4; break;
         case PCT_ARR_H_FAILED_CUTS: b = &c->h.failed; n = H; break;
-        case PCT_ARR_ROW_OFFSETS: b = &c->row_offsets; n = c->stage >= ST_ROWS ? (H + 1) * 8 : 0; break;
-        case PCT_ARR_ROWS: b = &c->rows; n = c->stage >= ST_ROWS ? (size_t)c->counts.row_entries * 4 : 0; break;
+        case PCT_ARR_ROW_OFFSETS: b = &c->dense_off; n = c->stage >= ST_ROWS ? (H + 1) * 8 : 0; break;
+        case PCT_ARR_ROWS: b = &c->dense_rows; n = c->stage >= ST_ROWS ? (size_t)c->dense_total * 4 : 0; break;
         case PCT_ARR_CHORD: b = &c->chord; n = c->stage >= ST_ROWS ? H * 4 : 0; break;
         default: return pct_fail(PCT_ERR_ARGUMENT, "unknown array %d", (int)which);
     }

@@ -109,8 +109,10 @@ struct pct_ctx {
     DevBuf fbp_image, fbp_hull, x_hull, x_hull_filtered, x0, x, x_update;
 
     /* MLP rows and DROP */
-    DevBuf row_offsets, rows, chord, inv_norm, mlp_table;
+    DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
     DevBuf block_diag, block_diag_offsets;
+    DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
+    int64_t dense_total = 0;
     DevBuf drop_resid;
     cudaGraphExec_t drop_graph_exec = nullptr;  /* one DROP iteration */
     int64_t row_capacity = 0;
@@ -148,5 +150,7 @@ enum { ERR_WALK_CAPPED = 0, ERR_VOXEL_OUTSIDE = 1, ERR_FIXED_OVERFLOW = 2, ERR_R
 
 DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g);
 void pct_drop_release_graph(pct_ctx* c);
+pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* off, int64_t* total);
+pct_status pct_rows_dense(pct_ctx* c, int64_t* total, DevBuf* dense_off, DevBuf* dense);
 
 #endif

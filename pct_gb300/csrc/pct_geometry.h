@@ -98,6 +98,8 @@ PCT_GFN void pct_config_fill_defaults(pct_config* c) {
     c->lambda = 0.001f;
     c->residual_tol = 0.0;
     c->chord_bf16 = 0;
+    c->mlp_exact = 0;
+    c->mlp_face_margin = 2e-5;
 }
 
 /* Returns 0 on success, nonzero when a derived size is out of range. */

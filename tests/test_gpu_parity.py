@@ -142,6 +142,26 @@ def test_mlp_rows_bit_exact(run):
     assert same(out["CHORD"], chord.astype(np.float32))
 
 
+def test_mlp_fast_path_used_and_exact_mode_agrees(run):
+    """The binary32 path must do most samples; an all-binary64 run must give the same rows."""
+    name, cfg, ora, out = run
+    c = out["counts"]
+    total_samples = int(out["ROW_OFFSETS"][-1])
+    assert c["mlp_fp64_samples"] < 0.2 * max(total_samples, 1), c
+    cfg2 = phantoms.make_config({})
+    for f, _ in cfg._fields_:
+        setattr(cfg2, f, getattr(cfg, f))
+    cfg2.mlp_exact = 1
+    w, _ = CASES[name]()
+    data, angles = phantoms.generate(w)
+    r = recon.run_full(cfg2, data, angles)
+    r.collect_mlp_endpoints()
+    r.mlp_rows()
+    rows = r.array("ROWS")
+    r.close()
+    assert same(rows, out["ROWS"])
+
+
 def test_drop_within_tolerance_of_fp64(run):
     name, cfg, ora, out = run
     its = cfg.iterations
