@@ -239,6 +239,29 @@ pct_status pct_set_image(pct_ctx* ctx, const float* x);
 /* CUDA stream the context runs on (cudaStream_t). */
 void* pct_stream(pct_ctx* ctx);
 
+/* DROP without allocation.  No counterpart in the reference (its DROP always
+ * allocates per-iteration buffers with cudaMalloc, .cu:6795-6860).
+ *
+ * For callers that may not allocate during the call: a process on a locked,
+ * pre-sized memory pool, or one that must not let cudaMalloc/cudaFree
+ * synchronise the device in the middle of its own stream sequence.  The call
+ * runs `iterations` DROP iterations in blocks of block_size histories on
+ * caller-owned DEVICE arrays (dense CSR rows: row_offsets has n+1 entries,
+ * rows holds voxel indices, entries >= num_voxels are skipped) and updates x
+ * in place on `stream` (a cudaStream_t; NULL = legacy default stream); it
+ * does not synchronise.  residual_sq (device, `iterations` doubles, may be
+ * NULL) receives sum_i (b_i - c_i a_i.x)^2 of each sweep.  Per-voxel scratch is
+ * a static device array of PCT_NOALLOC_MAX_VOXELS voxels: larger images are
+ * rejected with PCT_ERR_ARGUMENT.  Calls that overlap on one device share that
+ * scratch and race.  The first call on a device (or pct_noalloc_setup() with
+ * that device current) looks the scratch up and may load the module, so make
+ * it before any stream capture. */
+#define PCT_NOALLOC_MAX_VOXELS (1 << 21)
+pct_status pct_noalloc_setup(void);
+pct_status pct_drop_noalloc(int64_t n, const int64_t* row_offsets, const uint32_t* rows, const float* chord,
+                            const float* wepl, int num_voxels, int block_size, float lambda, int iterations,
+                            float* x, double* residual_sq, void* stream);
+
 pct_status pct_config_default(pct_config* cfg);
 pct_status pct_geometry_from_config(const pct_config* cfg, pct_geometry* geo);
 const char* pct_last_error(void);
