@@ -321,117 +321,283 @@ __device__ __forceinline__ int dev_sample_count(const MlpTableEntry* __restrict_
     return lo;
 }
 
+/* Per-history MLP constants: the binary64 setup (for the binary64 samples)
+ * and the binary32 Taylor coefficients b_m of the scattering power. */
+struct __align__(16) MlpRec {
+    MlpSetup m;   /* 104 bytes */
+    float b[6];
+};
+static_assert(sizeof(MlpRec) == 128, "MlpRec layout");
+
+/* A sample whose voxel the binary32 path cannot certify: recomputed in
+ * binary64 by k_mlp_fix, one thread per sample. */
+struct MlpDeferred {
+    int64_t pos;   /* entry of the row slot holding the sample's voxel */
+    int64_t hist;
+    int k;
+    int pad;
+};
+
 __global__ void __launch_bounds__(256) k_mlp_bound(DevGeom g, int64_t n, HistView h,
                                                    const MlpTableEntry* __restrict__ tab, int kmax,
-                                                   int64_t* __restrict__ bound) {
+                                                   int64_t* __restrict__ bound, MlpRec* __restrict__ rec) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    MlpSetup m;
-    dev_mlp_setup(h, i, m);
-    bound[i] = (int64_t)dev_sample_count(tab, kmax, m.u_2, g.mlp_u_step) + 1;
-}
-
-__device__ __forceinline__ float face_distance(float pos, float zero, float size, float inv_size) {
-    float q = fabsf(pos - zero) * inv_size;
-    float fr = q - floorf(q);
-    return fminf(fr, 1.0f - fr) * size;
-}
-
-__global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, HistView h,
-                                                  const MlpTableEntry* __restrict__ tab, int kmax, float margin,
-                                                  const int64_t* __restrict__ row_start, uint32_t* __restrict__ rows,
-                                                  int* __restrict__ row_len, unsigned long long* __restrict__ flags) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    MlpSetup m;
-    dev_mlp_setup(h, i, m);
-    const int K = dev_sample_count(tab, kmax, m.u_2, g.mlp_u_step);
+    MlpRec r;
+    dev_mlp_setup(h, i, r.m);
+    bound[i] = (int64_t)dev_sample_count(tab, kmax, r.m.u_2, g.mlp_u_step) + 1;
     /* Taylor coefficients of the scattering power around u_2 (binary64, then float) */
     const double A[6] = {A0, PCT_A1_M * PCT_A1_P, PCT_A2_M * PCT_A2_P, PCT_A3_M * PCT_A3_P, PCT_A4_M * PCT_A4_P,
                          PCT_A5_M * PCT_A5_P};
-    float b[6];
 #pragma unroll
     for (int mm = 0; mm < 6; ++mm) {
         double sum = 0.0, up = 1.0, binom = 1.0;
         for (int k = mm; k < 6; ++k) {
             sum += binom * A[k] * up;
-            up *= m.u_2;
+            up *= r.m.u_2;
             binom = binom * (k + 1) / (k + 1 - mm);
         }
-        b[mm] = (float)((mm & 1) ? -sum : sum);
+        r.b[mm] = (float)((mm & 1) ? -sum : sum);
     }
-    const float u2_hi = (float)m.u_2, u2_lo = (float)(m.u_2 - (double)u2_hi);
-    const float dT = (float)(m.T20 - m.T0), dV = (float)(m.V20 - m.V0);
-    const float T21 = (float)m.T21, V21 = (float)m.V21;
-    const float cef = (float)m.ce, sef = (float)m.se;
-    const float x_in = h.x_entry[i], y_in = h.y_entry[i], V0 = (float)m.V0;
-    /* x at depth u_1 on the entry line: x_in + ce u_1 (the entry point has depth 0) */
+    rec[i] = r;
+}
+
+/* dev_mlp_voxel out of line, for the rare binary64 samples of k_mlp_fast (keeps
+ * the binary32 loop's register footprint small). */
+__device__ __noinline__ uint32_t dev_mlp_voxel_rec(DevGeom g, const MlpRec* __restrict__ r, double u_1) {
+    MlpSetup m = r->m;
+    return (uint32_t)dev_mlp_voxel(g, m, u_1);
+}
+
+/* Classification of one binary32 sample. */
+enum { SAMPLE_CERTAIN = 0, SAMPLE_PAIR = 1, SAMPLE_EXACT = 2 };
+
+struct MlpSample {
+    int state;
+    uint32_t v;      /* CERTAIN: the voxel; PAIR: one candidate */
+    uint32_t v_alt;  /* PAIR: the candidate across the near face */
+};
+
+/* Voxel index along one axis from a binary32 coordinate; *amb is -1 / +1 when
+ * the coordinate lies within `margin` of the lower / upper face of that voxel. */
+__device__ __forceinline__ int axis_index(float pos, float zero, float size, float inv_size, float margin, int* amb) {
+    float q = fabsf(pos - zero) * inv_size;
+    int i0 = (int)q;
+    float fr = q - (float)i0;
+    *amb = fr * size < margin ? -1 : ((1.0f - fr) * size < margin ? 1 : 0);
+    return i0;
+}
+
+struct MlpFast {
+    float b[6];
+    float u2_hi, u2_lo, dT, dV, T21, V21, cef, sef, x_in, y_in, V0;
+};
+
+__device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpFast& f, const MlpTableEntry te,
+                                                   float margin) {
     const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
     const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
     const float iVW = 1.0f / VW, iVH = 1.0f / VH, iVT = 1.0f / VT;
     const float lnX0 = __logf(36.08f);
+    const float* b = f.b;
+    float d = (f.u2_hi - te.u1_hi) + (f.u2_lo - te.u1_lo);
+    float k2 = 13.6f * (1.0f + 0.038f * (__logf(d) - lnX0));
+    float c2 = k2 * k2 * (1.0f / 36.08f);
+    float Q1 = b[5] * (1.0f / 6), Q2 = b[5] * (1.0f / 7), Q3 = b[5] * (1.0f / 8);
+    Q1 = fmaf(Q1, d, b[4] * (1.0f / 5)); Q2 = fmaf(Q2, d, b[4] * (1.0f / 6)); Q3 = fmaf(Q3, d, b[4] * (1.0f / 7));
+    Q1 = fmaf(Q1, d, b[3] * (1.0f / 4)); Q2 = fmaf(Q2, d, b[3] * (1.0f / 5)); Q3 = fmaf(Q3, d, b[3] * (1.0f / 6));
+    Q1 = fmaf(Q1, d, b[2] * (1.0f / 3)); Q2 = fmaf(Q2, d, b[2] * (1.0f / 4)); Q3 = fmaf(Q3, d, b[2] * (1.0f / 5));
+    Q1 = fmaf(Q1, d, b[1] * (1.0f / 2)); Q2 = fmaf(Q2, d, b[1] * (1.0f / 3)); Q3 = fmaf(Q3, d, b[1] * (1.0f / 4));
+    Q1 = fmaf(Q1, d, b[0]);              Q2 = fmaf(Q2, d, b[0] * (1.0f / 2)); Q3 = fmaf(Q3, d, b[0] * (1.0f / 3));
+    /* E1 = Q1 - Q2 (weights 1/((m+1)(m+2))), E2 = Q1 - 2 Q2 + Q3, E3 = Q2 - Q3, each summed directly */
+    float E1 = b[5] * (1.0f / 42), E2 = b[5] * (2.0f / 336), E3 = b[5] * (1.0f / 56);
+    E1 = fmaf(E1, d, b[4] * (1.0f / 30)); E2 = fmaf(E2, d, b[4] * (2.0f / 210)); E3 = fmaf(E3, d, b[4] * (1.0f / 42));
+    E1 = fmaf(E1, d, b[3] * (1.0f / 20)); E2 = fmaf(E2, d, b[3] * (2.0f / 120)); E3 = fmaf(E3, d, b[3] * (1.0f / 30));
+    E1 = fmaf(E1, d, b[2] * (1.0f / 12)); E2 = fmaf(E2, d, b[2] * (2.0f / 60));  E3 = fmaf(E3, d, b[2] * (1.0f / 20));
+    E1 = fmaf(E1, d, b[1] * (1.0f / 6));  E2 = fmaf(E2, d, b[1] * (2.0f / 24));  E3 = fmaf(E3, d, b[1] * (1.0f / 12));
+    E1 = fmaf(E1, d, b[0] * (1.0f / 2));  E2 = fmaf(E2, d, b[0] * (2.0f / 6));   E3 = fmaf(E3, d, b[0] * (1.0f / 6));
+    float D = fmaf(Q3, Q1, -Q2 * Q2);
+    float inv = 1.0f / (c2 * D);
+    float id = 1.0f / d;
+    float id2 = id * id, id3 = id2 * id;
+    float Aa = Q1 * inv * id3;      /* (Sigma_2^-1)_00 */
+    float Bm = E1 * inv * id2;      /* (R1^T Sigma_2^-1 R1)_01 */
+    float Cm = E2 * inv * id;       /* (R1^T Sigma_2^-1 R1)_11 */
+    float bb = -Q2 * inv * id2;     /* (Sigma_2^-1)_01 */
+    float e3 = -E3 * inv * id;      /* d (Sigma_2^-1)_01 + (Sigma_2^-1)_11 */
+    float ft0 = te.s1i0 + Aa, ft1 = te.s1i1 + Bm, ft3 = te.s1i3 + Cm;
+    float idet = 1.0f / fmaf(ft0, ft3, -ft1 * ft1);
+    float beta = fmaf(ft3, Aa, -ft1 * Bm) * idet;
+    float gam = fmaf(ft3, bb, -ft1 * e3) * idet;
+    float ct = fmaf(beta, f.dT, gam * f.T21);
+    float cv = fmaf(beta, f.dV, gam * f.V21);
+    float u1f = te.u1_hi;
+    float x1 = f.x_in + fmaf(f.cef, u1f, -f.sef * ct);
+    float y1 = f.y_in + fmaf(f.sef, u1f, f.cef * ct);
+    float z1 = f.V0 + cv;
+    MlpSample s;
+    s.v = s.v_alt = 0;
+    if (!(fabsf(ct) < 1e3f) || !(fabsf(cv) < 1e3f)) {
+        s.state = SAMPLE_EXACT;
+        return s;
+    }
+    int ax, ay, az;
+    int vx = axis_index(x1, X0, VW, iVW, margin, &ax);
+    int vy = axis_index(y1, Y0, VH, iVH, margin, &ay);
+    int vz = axis_index(z1, Z0, VT, iVT, margin, &az);
+    const int C = g.columns, CR = g.columns * g.rows;
+    s.v = (uint32_t)(vx + vy * C + vz * CR);
+    int namb = (ax != 0) + (ay != 0) + (az != 0);
+    if (namb == 0) {
+        s.state = SAMPLE_CERTAIN;
+    } else if (namb == 1) {
+        s.state = SAMPLE_PAIR;
+        s.v_alt = (uint32_t)((vx + ax) + (vy + ay) * C + (vz + az) * CR);
+    } else {
+        s.state = SAMPLE_EXACT;
+    }
+    return s;
+}
+
+/* Fills the row slot of each history.  A sample within `margin` of a voxel
+ * face has two candidate voxels; when they are exactly the previous row entry
+ * and the (certain) next sample's voxel, either choice gives the same row
+ * after consecutive repeats are dropped, so the sample is skipped.  Any other
+ * uncertain sample gets a placeholder entry, is queued for k_mlp_fix, and the
+ * next sample is written unconditionally; k_mlp_dedupe then drops the repeats
+ * around the resolved entries.  With exact != 0 every sample is binary64. */
+__global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const MlpRec* __restrict__ rec,
+                                                  const uint32_t* __restrict__ first_voxel,
+                                                  const float* __restrict__ x_entry, const float* __restrict__ y_entry,
+                                                  const MlpTableEntry* __restrict__ tab, int kmax, float margin,
+                                                  int exact, const int64_t* __restrict__ row_start,
+                                                  uint32_t* __restrict__ rows, int* __restrict__ row_len,
+                                                  MlpDeferred* __restrict__ queue, int64_t queue_cap,
+                                                  int64_t* __restrict__ fix_rows,
+                                                  unsigned long long* __restrict__ flags) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const MlpRec& R = rec[i];
+    const double u_2 = R.m.u_2;
+    const int K = dev_sample_count(tab, kmax, u_2, g.mlp_u_step);
+    const uint32_t nv = (uint32_t)g.num_voxels;
     int64_t out = row_start[i];
     int len = 0;
-    uint32_t prev = h.first_voxel[i];
+    uint32_t prev = first_voxel[i];
     rows[out + len++] = prev;
-    int exact_samples = 0, outside = prev >= (uint32_t)g.num_voxels;
-    for (int k = 0; k < K; ++k) {
-        const MlpTableEntry te = tab[k];
-        float d = (u2_hi - te.u1_hi) + (u2_lo - te.u1_lo);
-        float k2 = 13.6f * (1.0f + 0.038f * (__logf(d) - lnX0));
-        float c2 = k2 * k2 * (1.0f / 36.08f);
-        float Q1 = b[5] * (1.0f / 6), Q2 = b[5] * (1.0f / 7), Q3 = b[5] * (1.0f / 8);
-        Q1 = fmaf(Q1, d, b[4] * (1.0f / 5)); Q2 = fmaf(Q2, d, b[4] * (1.0f / 6)); Q3 = fmaf(Q3, d, b[4] * (1.0f / 7));
-        Q1 = fmaf(Q1, d, b[3] * (1.0f / 4)); Q2 = fmaf(Q2, d, b[3] * (1.0f / 5)); Q3 = fmaf(Q3, d, b[3] * (1.0f / 6));
-        Q1 = fmaf(Q1, d, b[2] * (1.0f / 3)); Q2 = fmaf(Q2, d, b[2] * (1.0f / 4)); Q3 = fmaf(Q3, d, b[2] * (1.0f / 5));
-        Q1 = fmaf(Q1, d, b[1] * (1.0f / 2)); Q2 = fmaf(Q2, d, b[1] * (1.0f / 3)); Q3 = fmaf(Q3, d, b[1] * (1.0f / 4));
-        Q1 = fmaf(Q1, d, b[0]);              Q2 = fmaf(Q2, d, b[0] * (1.0f / 2)); Q3 = fmaf(Q3, d, b[0] * (1.0f / 3));
-        /* E1 = Q1 - Q2 (weights 1/((m+1)(m+2))), E2 = Q1 - 2 Q2 + Q3, E3 = Q2 - Q3, each summed directly */
-        float E1 = b[5] * (1.0f / 42), E2 = b[5] * (2.0f / 336), E3 = b[5] * (1.0f / 56);
-        E1 = fmaf(E1, d, b[4] * (1.0f / 30)); E2 = fmaf(E2, d, b[4] * (2.0f / 210)); E3 = fmaf(E3, d, b[4] * (1.0f / 42));
-        E1 = fmaf(E1, d, b[3] * (1.0f / 20)); E2 = fmaf(E2, d, b[3] * (2.0f / 120)); E3 = fmaf(E3, d, b[3] * (1.0f / 30));
-        E1 = fmaf(E1, d, b[2] * (1.0f / 12)); E2 = fmaf(E2, d, b[2] * (2.0f / 60));  E3 = fmaf(E3, d, b[2] * (1.0f / 20));
-        E1 = fmaf(E1, d, b[1] * (1.0f / 6));  E2 = fmaf(E2, d, b[1] * (2.0f / 24));  E3 = fmaf(E3, d, b[1] * (1.0f / 12));
-        E1 = fmaf(E1, d, b[0] * (1.0f / 2));  E2 = fmaf(E2, d, b[0] * (2.0f / 6));   E3 = fmaf(E3, d, b[0] * (1.0f / 6));
-        float D = fmaf(Q3, Q1, -Q2 * Q2);
-        float inv = 1.0f / (c2 * D);
-        float id = 1.0f / d;
-        float id2 = id * id, id3 = id2 * id;
-        float Aa = Q1 * inv * id3;      /* (Sigma_2^-1)_00 */
-        float Bm = E1 * inv * id2;      /* (R1^T Sigma_2^-1 R1)_01 */
-        float Cm = E2 * inv * id;       /* (R1^T Sigma_2^-1 R1)_11 */
-        float bb = -Q2 * inv * id2;     /* (Sigma_2^-1)_01 */
-        float e3 = -E3 * inv * id;      /* d (Sigma_2^-1)_01 + (Sigma_2^-1)_11 */
-        float ft0 = te.s1i0 + Aa, ft1 = te.s1i1 + Bm, ft3 = te.s1i3 + Cm;
-        float idet = 1.0f / fmaf(ft0, ft3, -ft1 * ft1);
-        float beta = fmaf(ft3, Aa, -ft1 * Bm) * idet;
-        float gam = fmaf(ft3, bb, -ft1 * e3) * idet;
-        float ct = fmaf(beta, dT, gam * T21);
-        float cv = fmaf(beta, dV, gam * V21);
-        float u1f = te.u1_hi;
-        float x1 = x_in + fmaf(cef, u1f, -sef * ct);
-        float y1 = y_in + fmaf(sef, u1f, cef * ct);
-        float z1 = V0 + cv;
-        uint32_t v;
-        if (face_distance(x1, X0, VW, iVW) < margin || face_distance(y1, Y0, VH, iVH) < margin ||
-            face_distance(z1, Z0, VT, iVT) < margin || !(fabsf(ct) < 1e3f) || !(fabsf(cv) < 1e3f)) {
-            v = (uint32_t)dev_mlp_voxel(g, m, te.u1);
-            ++exact_samples;
-        } else {
-            int vx = (int)(fabsf(x1 - X0) * iVW);
-            int vy = (int)(fabsf(y1 - Y0) * iVH);
-            int vz = (int)(fabsf(z1 - Z0) * iVT);
-            v = (uint32_t)(vx + vy * g.columns + vz * g.columns * g.rows);
+    int fp64_samples = 0, deferred = 0, outside = prev >= nv;
+    if (exact) {
+        for (int k = 0; k < K; ++k) {
+            uint32_t v = dev_mlp_voxel_rec(g, &R, tab[k].u1);
+            ++fp64_samples;
+            if (v != prev) {
+                rows[out + len++] = v;
+                prev = v;
+                outside += v >= nv;
+            }
         }
-        if (v != prev) {
-            rows[out + len++] = v;
-            prev = v;
-            outside += v >= (uint32_t)g.num_voxels;
+    } else {
+        MlpFast f;
+#pragma unroll
+        for (int mm = 0; mm < 6; ++mm) f.b[mm] = R.b[mm];
+        f.u2_hi = (float)u_2;
+        f.u2_lo = (float)(u_2 - (double)f.u2_hi);
+        f.dT = (float)(R.m.T20 - R.m.T0);
+        f.dV = (float)(R.m.V20 - R.m.V0);
+        f.T21 = (float)R.m.T21;
+        f.V21 = (float)R.m.V21;
+        f.cef = (float)R.m.ce;
+        f.sef = (float)R.m.se;
+        f.x_in = x_entry[i];
+        f.y_in = y_entry[i];
+        f.V0 = (float)R.m.V0;
+        int force = 0; /* the last entry is a placeholder: write the next voxel whatever it is */
+        MlpSample cur = K > 0 ? dev_mlp_sample(g, f, tab[0], margin) : MlpSample{SAMPLE_CERTAIN, 0u, 0u};
+        for (int k = 0; k < K; ++k) {
+            MlpSample nxt{SAMPLE_EXACT, 0u, 0u};
+            if (k + 1 < K) nxt = dev_mlp_sample(g, f, tab[k + 1], margin);
+            if (cur.state == SAMPLE_CERTAIN) {
+                if (force || cur.v != prev) {
+                    rows[out + len++] = cur.v;
+                    prev = cur.v;
+                    outside += cur.v >= nv;
+                    force = 0;
+                }
+            } else if (cur.state == SAMPLE_PAIR && !force && nxt.state == SAMPLE_CERTAIN &&
+                       ((cur.v == prev && cur.v_alt == nxt.v) || (cur.v_alt == prev && cur.v == nxt.v))) {
+                /* either candidate drops out with the repeats */
+            } else {
+                ++fp64_samples;
+                unsigned long long slot = atomicAdd(flags + ERR_MLP_QUEUED, 1ull);
+                if ((int64_t)slot < queue_cap) {
+                    MlpDeferred q;
+                    q.pos = out + len;
+                    q.hist = i;
+                    q.k = k;
+                    q.pad = 0;
+                    queue[slot] = q;
+                    rows[out + len++] = 0u;
+                    ++deferred;
+                    force = 1;
+                } else {
+                    /* queue full: binary64 here */
+                    uint32_t v = dev_mlp_voxel_rec(g, &R, tab[k].u1);
+                    if (force || v != prev) {
+                        rows[out + len++] = v;
+                        prev = v;
+                        outside += v >= nv;
+                        force = 0;
+                    }
+                }
+            }
+            cur = nxt;
         }
     }
     row_len[i] = len;
-    if (exact_samples) atomicAdd(flags + ERR_MLP_FP64, (unsigned long long)exact_samples);
-    if (outside) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
+    if (deferred) {
+        unsigned long long r = atomicAdd(flags + ERR_MLP_FIXROWS, 1ull);
+        fix_rows[r] = i; /* r < number of queued samples <= queue_cap */
+    } else if (outside) {
+        atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
+    }
+    if (fp64_samples) atomicAdd(flags + ERR_MLP_FP64, (unsigned long long)fp64_samples);
+}
+
+/* The queued samples in binary64, one thread each. */
+__global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __restrict__ rec,
+                                                 const MlpTableEntry* __restrict__ tab,
+                                                 const MlpDeferred* __restrict__ queue, int64_t queue_cap,
+                                                 const unsigned long long* __restrict__ flags,
+                                                 uint32_t* __restrict__ rows) {
+    int64_t count = (int64_t)flags[ERR_MLP_QUEUED];
+    if (count > queue_cap) count = queue_cap;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+        MlpDeferred d = queue[q];
+        MlpSetup m = rec[d.hist].m;
+        rows[d.pos] = (uint32_t)dev_mlp_voxel(g, m, tab[d.k].u1);
+    }
+}
+
+/* Drops consecutive repeats in the rows that had queued samples. */
+__global__ void k_mlp_dedupe(int64_t queue_cap, const int64_t* __restrict__ fix_rows,
+                             const int64_t* __restrict__ row_start, int* __restrict__ row_len,
+                             uint32_t* __restrict__ rows, uint32_t nv, unsigned long long* __restrict__ flags) {
+    int64_t count = (int64_t)flags[ERR_MLP_FIXROWS];
+    if (count > queue_cap) count = queue_cap;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < count; r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = fix_rows[r];
+        uint32_t* row = rows + row_start[i];
+        int len = row_len[i], w = 1, outside = row[0] >= nv;
+        for (int j = 1; j < len; ++j) {
+            uint32_t v = row[j];
+            if (v != row[w - 1]) {
+                row[w++] = v;
+                outside += v >= nv;
+            }
+        }
+        row_len[i] = w;
+        if (outside) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
+    }
 }
 
 /* Dense copy of the bounded rows (for pct_get_array). */
@@ -604,22 +770,34 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
     int64_t bound_total = 0;
     HistView h = c->view(c->h);
     unsigned long long* flags = c->err_flags.as<unsigned long long>();
+    /* this call's sample counters start from zero */
+    PCT_CUDA(cudaMemsetAsync(flags + ERR_MLP_FP64, 0, sizeof(unsigned long long) * 4, c->stream));
     if (n > 0) {
-        DevBuf bound;
-        PCT_TRY(bound.alloc(sizeof(int64_t) * n));
+        PCT_TRY(c->mlp_bound.alloc(sizeof(int64_t) * n));
+        PCT_TRY(c->mlp_rec.alloc(sizeof(MlpRec) * n));
+        const int64_t queue_cap = n / 8 > (1 << 20) ? n / 8 : (1 << 20);
+        PCT_TRY(c->mlp_queue.alloc(sizeof(MlpDeferred) * queue_cap));
+        PCT_TRY(c->mlp_fix_rows.alloc(sizeof(int64_t) * queue_cap));
+        MlpRec* rec = c->mlp_rec.as<MlpRec>();
         ++c->launches;
         k_mlp_bound<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->mlp_table.as<MlpTableEntry>(), kmax,
-                                                                 bound.as<int64_t>());
-        pct_status st = pct_scan_lengths(c, bound.as<int64_t>(), n, c->row_offsets.as<int64_t>(), &bound_total);
-        c->launches += 3;
-        bound.release();
-        PCT_TRY(st);
+                                                                 c->mlp_bound.as<int64_t>(), rec);
+        PCT_TRY(pct_scan_lengths(c, c->mlp_bound.as<int64_t>(), n, c->row_offsets.as<int64_t>(), &bound_total));
         PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (bound_total > 0 ? bound_total : 1)));
-        float margin = c->cfg.mlp_exact ? 3.0e38f : (float)c->cfg.mlp_face_margin;
+        const int exact = c->cfg.mlp_exact != 0;
+        const float margin = (float)c->cfg.mlp_face_margin;
         ++c->launches;
-        k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, h, c->mlp_table.as<MlpTableEntry>(), kmax,
-                                                                margin, c->row_offsets.as<int64_t>(),
-                                                                c->rows.as<uint32_t>(), c->row_len.as<int>(), flags);
+        k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
+            c->dg, n, rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
+            c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(),
+            c->mlp_queue.as<MlpDeferred>(), queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
+        c->launches += 2;
+        k_mlp_fix<<<4 * 152, 128, 0, c->stream>>>(c->dg, rec, c->mlp_table.as<MlpTableEntry>(),
+                                                  c->mlp_queue.as<MlpDeferred>(), queue_cap, flags,
+                                                  c->rows.as<uint32_t>());
+        k_mlp_dedupe<<<2 * 152, 128, 0, c->stream>>>(queue_cap, c->mlp_fix_rows.as<int64_t>(),
+                                                     c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+                                                     c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels, flags);
         ++c->launches;
         k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(),
                                                                  c->chord.as<float>(), c->inv_norm.as<double>());

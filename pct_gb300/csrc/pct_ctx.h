@@ -110,6 +110,7 @@ struct pct_ctx {
 
     /* MLP rows and DROP */
     DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
+    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows;             /* MLP row generation scratch */
     DevBuf block_diag, block_diag_offsets;
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
     int64_t dense_total = 0;
@@ -146,7 +147,7 @@ pct_status pct_compact_histories(pct_ctx* c, const uint8_t* d_keep, int64_t n, i
 
 /* Device error counters (indices into err_flags, uint64). */
 enum { ERR_WALK_CAPPED = 0, ERR_VOXEL_OUTSIDE = 1, ERR_FIXED_OVERFLOW = 2, ERR_ROW_OVERFLOW = 3,
-       ERR_MLP_FP64 = 4, ERR_ROWS_OUTSIDE = 5, ERR_COUNT = 8 };
+       ERR_MLP_FP64 = 4, ERR_ROWS_OUTSIDE = 5, ERR_MLP_QUEUED = 6, ERR_MLP_FIXROWS = 7, ERR_COUNT = 8 };
 
 DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g);
 void pct_drop_release_graph(pct_ctx* c);
