@@ -97,7 +97,14 @@ typedef struct pct_config {
     int mlp_exact;                 /* 1: every MLP sample in binary64 (slow path, for checks) */
     double mlp_face_margin;        /* [cm] binary32 MLP samples closer than this to a voxel face
                                       are recomputed in binary64 (default 2e-5) */
+    int drop_form;                 /* DROP block step: PCT_DROP_AGGREGATED (default) or PCT_DROP_SCATTER */
 } pct_config;
+
+/* DROP block step forms.  AGGREGATED visits each block's rows in sinogram bin
+ * order and sums their updates per voxel in shared memory before adding them
+ * to the image; SCATTER adds every row entry's update with its own atomic.
+ * Both compute the same block update (binary32 sums in a different order). */
+enum { PCT_DROP_AGGREGATED = 0, PCT_DROP_SCATTER = 2 };
 
 /* Geometry derived from a pct_config, as the reference macros derive it. */
 typedef struct pct_geometry {

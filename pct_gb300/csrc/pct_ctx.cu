@@ -246,6 +246,8 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     int e = pct_geometry_derive(cfg, &g);
     if (e) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: invalid geometry (code %d)", e);
     if (cfg->block_size <= 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: block_size must be positive");
+    if (cfg->drop_form < 0 || cfg->drop_form > PCT_DROP_SCATTER)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_form %d", cfg->drop_form);
     if (cfg->mlp_hull < 0 || cfg->mlp_hull > 3) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: bad mlp_hull");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -285,7 +287,8 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->sc_hull, &c->msc_counts, &c->sm_counts, &c->msc_hull, &c->sm_hull, &c->fbp_image,
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
                      &c->rows, &c->chord, &c->inv_norm, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
-                     &c->drop_resid};
+                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows,
+                     &c->drop_perm, &c->drop_sort};
     for (DevBuf* b : all) b->release();
     for (auto& b : c->in13) b.release();
     pct_drop_release_graph(c);

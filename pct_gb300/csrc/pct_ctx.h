@@ -111,7 +111,8 @@ struct pct_ctx {
     /* MLP rows and DROP */
     DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
     DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows;             /* MLP row generation scratch */
-    DevBuf block_diag, block_diag_offsets;
+    DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
+    DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
     int64_t dense_total = 0;
     DevBuf drop_resid;
@@ -119,6 +120,7 @@ struct pct_ctx {
     int64_t row_capacity = 0;
     int num_blocks = 0;
     int diag_ready = 0;
+    int drop_aggregated = 0;       /* DROP runs in the aggregated form (else scatter) */
 
     pct_status set_device() {
         cudaError_t e = cudaSetDevice(device);

@@ -173,3 +173,27 @@ def test_drop_within_tolerance_of_fp64(run):
     st = out["stats"]
     assert st.iterations_run == its
     assert all(np.isfinite(st.residual[k]) and st.residual[k] > 0 for k in range(its))
+
+
+def test_drop_scatter_form_within_tolerance(run):
+    """The atomic scatter form of the DROP block step (the fallback when the
+    transposed copy does not fit) against the same binary64 iterate."""
+    name, cfg, ora, out = run
+    its = cfg.iterations
+    if its == 0:
+        pytest.skip("no iterations")
+    cfg2 = phantoms.make_config({})
+    for f, _ in cfg._fields_:
+        setattr(cfg2, f, getattr(cfg, f))
+    cfg2.drop_form = 2
+    w, _ = CASES[name]()
+    data, angles = phantoms.generate(w)
+    r = recon.run_full(cfg2, data, angles)
+    r.collect_mlp_endpoints()
+    r.mlp_rows()
+    r.drop(its)
+    x = r.array("X").astype(np.float64)
+    r.close()
+    ref = ora["x_%d" % its]
+    err = np.linalg.norm(x - ref) / np.linalg.norm(ref)
+    assert err <= DROP_TOL, "relative L2 %.3e" % err
