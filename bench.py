@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=6000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--drop-form", type=int, default=0, choices=[0, 1, 2],
+                    help="DROP block step: 0 scatter (default), 1 sorted, 2 tiled")
     return ap.parse_args()
 
 
@@ -202,7 +204,9 @@ def main():
     dev = torch.device("cuda", local)
 
     w = phantoms.cfg2(num_histories=a.histories, seed=2 + rank)
-    cfg = phantoms.make_config(w.config)
+    over = dict(w.config)
+    over["drop_form"] = a.drop_form
+    cfg = phantoms.make_config(over)
     iters = cfg.iterations
     data, angles = phantoms.generate(w)
     n = data.shape[1]
@@ -256,8 +260,12 @@ def main():
     drop_iter_s = drop_s / (a.steps * iters)
 
     # ---- roofline of the dominant kernel ----------------------------------------------
-    # DROP iteration: per row 8 B offset + 4 B chord + 8 B 1/||a||^2 + 4 B WEPL, 4 B per
-    # row entry read; image gathers/scatters stay in L2 and are not counted.
+    # One DROP iteration (the dominant part of a step: 12 of them per MLP pass).
+    # Algorithmic bytes per recon history and iteration: 4 B WEPL + 8 B row start
+    # + 4 B chord + 8 B 1/||a||^2 + 4 B per row entry (voxel index); the image
+    # gathers and update reductions stay in L2 and are not counted.  The launch
+    # timed is one DROP iteration (all blocks: k_drop_rows + k_drop_relax per
+    # block in the scatter form) with CUDA events on the context stream.
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -265,17 +273,17 @@ def main():
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     drop_bytes = R * 24 + rows * 4
-    mlp_bytes = R * 48 + rows * 4 + (R + 1) * 8 * 2
-    if drop_s >= mlp_s:
-        achieved = drop_bytes / drop_iter_s / 1e9
-        dom = "k_drop_rows (one DROP iteration)"
-    else:
-        achieved = mlp_bytes / (mlp_s / a.steps) / 1e9
-        dom = "k_mlp_count+k_mlp_fill (MLP rows)"
+    achieved = drop_bytes / drop_iter_s / 1e9
+    forms = {0: "k_drop_rows + k_drop_relax (scatter)", 1: "k_drop_rows + k_drop_relax (sorted)",
+             2: "k_tile_fwd + k_tile_rows + k_tile_bwd (tiled)"}
+    dom = "one DROP iteration: %s" % forms[a.drop_form]
     traffic = None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
-        traffic = tr.get(dom.split()[0])
+        t = tr.get("drop_form_%d" % a.drop_form)
+        if t:  # DRAM bytes of one iteration, scaled from a smaller ncu capture
+            nblocks = (R + cfg.block_size - 1) // cfg.block_size
+            traffic = t["ratio_to_algorithmic"] * drop_bytes + t["per_block_bytes"] * nblocks
     except Exception:
         pass
 
@@ -324,12 +332,14 @@ def main():
                                    " block %d, lambda %.2g" % (n, R, iters, cfg.block_size, cfg.lambda_),
                        "row_entries": rows, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "inputs larger than L2 (MLP rows %.1f GB)" % (rows * 4 / 1e9),
-                       "mlp_ms_per_step": mlp_s / a.steps * 1e3, "drop_ms_per_iteration": drop_iter_s * 1e3},
+                       "drop_form": forms[a.drop_form],
+                       "rows_ms_per_step": mlp_s / a.steps * 1e3, "drop_ms_per_iteration": drop_iter_s * 1e3},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * 14 * 4),
                     "d2h_bytes_per_step": int(nv * 4), "seconds_per_step": e2e_t / a.e2e_steps},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"},
+                         "algorithmic_bytes": drop_bytes,
+                         "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"},
             "cpu_baseline": cpu_b, "gpu_launches": launches, "clocks": clocks,
         }
         print(json.dumps(out))

@@ -97,14 +97,17 @@ typedef struct pct_config {
     int mlp_exact;                 /* 1: every MLP sample in binary64 (slow path, for checks) */
     double mlp_face_margin;        /* [cm] binary32 MLP samples closer than this to a voxel face
                                       are recomputed in binary64 (default 2e-5) */
-    int drop_form;                 /* DROP block step: PCT_DROP_AGGREGATED (default) or PCT_DROP_SCATTER */
+    int drop_form;                 /* DROP block step: PCT_DROP_SCATTER (default), _SORTED or _TILED */
 } pct_config;
 
-/* DROP block step forms.  AGGREGATED visits each block's rows in sinogram bin
- * order and sums their updates per voxel in shared memory before adding them
- * to the image; SCATTER adds every row entry's update with its own atomic.
- * Both compute the same block update (binary32 sums in a different order). */
-enum { PCT_DROP_AGGREGATED = 0, PCT_DROP_SCATTER = 2 };
+/* DROP block step forms; all compute the same block update.  SCATTER adds
+ * every row entry's update with a binary32 reduction in L2.  SORTED is
+ * SCATTER with each block's rows visited in sinogram bin order.  TILED
+ * regroups each block's rows by image tile once, then gathers and
+ * accumulates in shared memory with exact integer sums, so the iterate is
+ * reproducible bit for bit (falls back to SCATTER when its memory is not
+ * free). */
+enum { PCT_DROP_SCATTER = 0, PCT_DROP_SORTED = 1, PCT_DROP_TILED = 2 };
 
 /* Geometry derived from a pct_config, as the reference macros derive it. */
 typedef struct pct_geometry {

@@ -13,15 +13,12 @@
  * in every iteration.  One CUDA graph holds the 2 * blocks launches of an
  * iteration.
  *
- * Aggregated form (default): the rows of each block are visited in sinogram
- * bin order (a per-block counting sort by bin, once per set of rows), and one
- * warp walks 32 consecutive rows in step, one per lane (k_drop_lanes).  Rows
- * of one bin follow nearly the same path, so the iterate gathers of a step
- * coalesce and the lanes on one voxel add their summed update with a single
- * L2 reduction.  The diagonal weights come from the same kernel adding 1 per
- * entry.
- * Scatter form: one warp per row in history order and one L2 reduction per
- * row entry (k_drop_rows), the direct transcription of the block update.
+ * Forms: the tiled form (k_drop_tiled.cu, default where it fits) regroups
+ * the rows by image tile; the scatter form runs one warp per row in history
+ * order with one L2 reduction per row entry (k_drop_rows + k_drop_relax), the
+ * direct transcription of the block update; the sorted form is the scatter
+ * form visiting each block's rows in sinogram bin order (a per-block
+ * counting sort, once per set of rows).
  */
 #include <cstring>
 #include "pct_device.cuh"
@@ -189,159 +186,6 @@ __global__ void k_sort_fill(int64_t start, int64_t end, const int32_t* __restric
     perm[start + off[key] + slot] = (uint32_t)(i - start);
 }
 
-/* Sum of val over this lane's run of equal v up to the run's end (runs are
- * maximal sequences of consecutive lanes with equal v), by a segmented suffix
- * scan; the run's first lane gets the whole run's sum. */
-__device__ __forceinline__ float run_sum(uint32_t v, float val, int lane, int* is_head) {
-    uint32_t nxt = __shfl_down_sync(0xffffffffu, v, 1);
-    uint32_t prv = __shfl_up_sync(0xffffffffu, v, 1);
-    int f = lane == 31 || nxt != v; /* a run ends inside this lane's window */
-    float sum = val;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        float ts = __shfl_down_sync(0xffffffffu, sum, o);
-        int tf = __shfl_down_sync(0xffffffffu, f, o);
-        if (!f) {
-            sum += ts;
-            f = tf;
-        }
-    }
-    *is_head = lane == 0 || prv != v;
-    return sum;
-}
-
-/* One warp: 32 consecutive rows of the block's bin order, one per lane, walked
- * entry by entry in step.  The rows are read in coalesced 32-entry chunks
- * (row by row) and transposed through shared memory.  Rows of one bin follow
- * nearly the same path, so at each step the lanes hold a few distinct voxels:
- * the iterate gathers coalesce, and each run of lanes on one voxel adds its
- * summed update with a single reduction.  COUNT: adds 1 per row entry (the
- * diagonal weights, exact in binary32 below 2^24); otherwise the block update
- * into out (x_update). */
-constexpr int LANE_WARPS = 4;
-constexpr uint32_t NO_VOXEL = 0xffffffffu;
-
-struct LaneRows {
-    int64_t a[32];
-    int len[32];
-    uint32_t buf[32][33];
-};
-
-/* Stages entries [k0, k0 + 32) of the warp's 32 rows: buf[r][e] = entry k0 + e of row r. */
-__device__ __forceinline__ void stage_chunk(LaneRows& L, const uint32_t* __restrict__ rows, int k0, int lane) {
-    __syncwarp();
-    for (int r = 0; r < 32; ++r) {
-        int k = k0 + lane;
-        L.buf[r][lane] = k < L.len[r] ? rows[L.a[r] + k] : NO_VOXEL;
-    }
-    __syncwarp();
-}
-
-template <bool COUNT>
-__global__ void __launch_bounds__(LANE_WARPS * 32) k_drop_lanes(int64_t start, int64_t end,
-                                                                const uint32_t* __restrict__ perm,
-                                                                const int64_t* __restrict__ row_start,
-                                                                const int* __restrict__ row_len,
-                                                                const uint32_t* __restrict__ rows,
-                                                                const float* __restrict__ chord,
-                                                                const double* __restrict__ inv_norm,
-                                                                const float* __restrict__ wepl, float lambda,
-                                                                const float* __restrict__ x, uint32_t nv,
-                                                                float* __restrict__ out, double* __restrict__ resid) {
-    __shared__ LaneRows lr[LANE_WARPS];
-    __shared__ double sres[LANE_WARPS];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    LaneRows& L = lr[w];
-    const int64_t j = start + ((int64_t)blockIdx.x * LANE_WARPS + w) * 32 + lane;
-    const bool have = j < end;
-    int64_t i = 0;
-    int len = 0;
-    if (have) {
-        i = start + perm[j];
-        L.a[lane] = row_start[i];
-        len = row_len[i];
-    } else {
-        L.a[lane] = 0;
-    }
-    L.len[lane] = len;
-    int maxlen = len;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        int t = __shfl_xor_sync(0xffffffffu, maxlen, o);
-        maxlen = t > maxlen ? t : maxlen;
-    }
-    float val = 1.0f;
-    double r2 = 0.0;
-    if (!COUNT) {
-        float dot = 0.0f;
-        for (int k0 = 0; k0 < maxlen; k0 += 32) {
-            stage_chunk(L, rows, k0, lane);
-#pragma unroll 4
-            for (int e = 0; e < 32; ++e) {
-                uint32_t v = L.buf[lane][e];
-                if (v < nv) dot += x[v];
-            }
-        }
-        if (have) {
-            double c = chord[i];
-            double res = (double)wepl[i] - c * (double)dot;
-            val = (float)(c * res * inv_norm[i] * (double)lambda);
-            r2 = res * res;
-        }
-    }
-    for (int k0 = 0; k0 < maxlen; k0 += 32) {
-        stage_chunk(L, rows, k0, lane);
-        int kend = maxlen - k0 < 32 ? maxlen - k0 : 32;
-        for (int e = 0; e < kend; ++e) {
-            uint32_t v = L.buf[lane][e];
-            float contrib = v < nv ? val : 0.0f;
-            int head;
-            float sum = run_sum(v, contrib, lane, &head);
-            if (head && v < nv) atomicAdd(out + v, sum);
-        }
-    }
-    if (!COUNT) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-        if (lane == 0) sres[w] = r2;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int k = 0; k < LANE_WARPS; ++k) t += sres[k];
-            if (t != 0.0) atomicAdd(resid, t);
-        }
-    }
-}
-
-/* x += x_update / s_j and x_update = 0 where s_j > 0; four voxels per thread
- * (float4 accesses when nv is a multiple of 4, else scalar). */
-__global__ void k_drop_relax4(int nv, const float* __restrict__ cnt, float* __restrict__ x, float* __restrict__ upd) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    int v0 = 4 * q;
-    if (v0 >= nv) return;
-    /* the block's weights start at k * nv floats: 16-byte aligned only when nv % 4 == 0 */
-    if ((nv & 3) == 0 && v0 + 3 < nv) {
-        float4 s = *reinterpret_cast<const float4*>(cnt + v0);
-        if (s.x == 0.0f && s.y == 0.0f && s.z == 0.0f && s.w == 0.0f) return;
-        float4 u = *reinterpret_cast<const float4*>(upd + v0);
-        float4 xv = *reinterpret_cast<float4*>(x + v0);
-        if (s.x > 0.0f) xv.x += u.x / s.x;
-        if (s.y > 0.0f) xv.y += u.y / s.y;
-        if (s.z > 0.0f) xv.z += u.z / s.z;
-        if (s.w > 0.0f) xv.w += u.w / s.w;
-        *reinterpret_cast<float4*>(x + v0) = xv;
-        *reinterpret_cast<float4*>(upd + v0) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    } else {
-        for (int v = v0; v < nv; ++v) {
-            float s = cnt[v];
-            if (s > 0.0f) {
-                x[v] += upd[v] / s;
-                upd[v] = 0.0f;
-            }
-        }
-    }
-}
-
 /* Moves the iteration's residual accumulator into its history slot. */
 __global__ void k_store_resid(double* __restrict__ acc, double* __restrict__ slot) {
     *slot = *acc;
@@ -384,17 +228,16 @@ static pct_status build_scatter(pct_ctx* c) {
     }
     PCT_CUDA(cudaGetLastError());
     c->num_blocks = nb;
-    c->drop_aggregated = 0;
+    c->drop_mode = PCT_DROP_SCATTER;
+    c->drop_launches_per_iter = 2 * nb;
     c->diag_ready = 1;
     return PCT_OK;
 }
 
-/* Bin order of every block and the per-block diagonal weights (binary32) for
- * the aggregated form. */
-static pct_status build_aggregated(pct_ctx* c) {
+/* Bin order of every block's rows for the sorted form (counts as in the scatter form). */
+static pct_status build_sorted(pct_ctx* c) {
     const int64_t n = c->h.n;
     const int64_t B = c->cfg.block_size;
-    const int nv = c->geo.num_voxels;
     const uint32_t nkeys = (uint32_t)c->geo.num_bins;
     const int tiles = (int)((nkeys + SCAN_TILE - 1) / SCAN_TILE);
     int nb = (int)((n + B - 1) / B);
@@ -415,19 +258,9 @@ static pct_status build_aggregated(pct_ctx* c) {
         k_scan_apply_u32<<<tiles, 1024, 0, c->stream>>>(cnt, nkeys, tsum, off);
         k_sort_fill<<<pct_grid_for(e - s, 256), 256, 0, c->stream>>>(s, e, bin, nkeys, cnt, off, perm);
     }
-    PCT_TRY(c->block_diag.alloc(sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1)));
-    PCT_CUDA(cudaMemsetAsync(c->block_diag.p, 0, sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
-    for (int k = 0; k < nb; ++k) {
-        int64_t s = k * B, e = s + B < n ? s + B : n;
-        ++c->launches;
-        k_drop_lanes<true><<<(unsigned)((e - s + LANE_WARPS * 32 - 1) / (LANE_WARPS * 32)), LANE_WARPS * 32, 0, c->stream>>>(
-            s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), nullptr,
-            nullptr, nullptr, 0.0f, nullptr, (uint32_t)nv, c->block_diag.as<float>() + (size_t)k * nv, nullptr);
-    }
     PCT_CUDA(cudaGetLastError());
-    c->num_blocks = nb;
-    c->drop_aggregated = c->cfg.drop_form == 1 ? 2 : 1;
-    c->diag_ready = 1;
+    PCT_TRY(build_scatter(c));
+    c->drop_mode = PCT_DROP_SORTED;
     return PCT_OK;
 }
 
@@ -438,35 +271,19 @@ static void enqueue_iteration(pct_ctx* c, double* resid) {
     const int nv = c->geo.num_voxels;
     for (int k = 0; k < c->num_blocks; ++k) {
         int64_t s = k * B, e = s + B < n ? s + B : n;
-        if (c->drop_aggregated == 2) {
-            unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
-            k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, c->drop_perm.as<uint32_t>(),
-                                                              c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
-                                                              c->rows.as<uint32_t>(), c->chord.as<float>(),
-                                                              c->inv_norm.as<double>(), c->h.wepl.as<float>(),
-                                                              c->cfg.lambda, c->x.as<float>(), c->x_update.as<float>(),
-                                                              (uint32_t)nv, resid);
-            k_drop_relax4<<<pct_grid_for((nv + 3) / 4, 256), 256, 0, c->stream>>>(
-                nv, c->block_diag.as<float>() + (size_t)k * nv, c->x.as<float>(), c->x_update.as<float>());
-        } else if (c->drop_aggregated) {
-            k_drop_lanes<false><<<(unsigned)((e - s + LANE_WARPS * 32 - 1) / (LANE_WARPS * 32)), LANE_WARPS * 32, 0,
-                                  c->stream>>>(
-                s, e, c->drop_perm.as<uint32_t>(), c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
-                c->rows.as<uint32_t>(), c->chord.as<float>(), c->inv_norm.as<double>(), c->h.wepl.as<float>(),
-                c->cfg.lambda, c->x.as<float>(), (uint32_t)nv, c->x_update.as<float>(), resid);
-            k_drop_relax4<<<pct_grid_for((nv + 3) / 4, 256), 256, 0, c->stream>>>(
-                nv, c->block_diag.as<float>() + (size_t)k * nv, c->x.as<float>(), c->x_update.as<float>());
-        } else {
-            unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
-            k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, nullptr, c->row_offsets.as<int64_t>(),
-                                                              c->row_len.as<int>(),
-                                                              c->rows.as<uint32_t>(), c->chord.as<float>(),
-                                                              c->inv_norm.as<double>(), c->h.wepl.as<float>(),
-                                                              c->cfg.lambda, c->x.as<float>(), c->x_update.as<float>(),
-                                                              (uint32_t)nv, resid);
-            k_drop_relax<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(nv, c->block_diag.as<uint32_t>() + (size_t)k * nv,
-                                                                       c->x.as<float>(), c->x_update.as<float>());
+        if (c->drop_mode == PCT_DROP_TILED) {
+            pct_drop_tiled_enqueue(c, k, resid);
+            continue;
         }
+        unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
+        const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
+        k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+                                                          c->rows.as<uint32_t>(), c->chord.as<float>(),
+                                                          c->inv_norm.as<double>(), c->h.wepl.as<float>(),
+                                                          c->cfg.lambda, c->x.as<float>(), c->x_update.as<float>(),
+                                                          (uint32_t)nv, resid);
+        k_drop_relax<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(nv, c->block_diag.as<uint32_t>() + (size_t)k * nv,
+                                                                   c->x.as<float>(), c->x_update.as<float>());
     }
 }
 
@@ -490,9 +307,24 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
     if (iterations < 0) return pct_fail(PCT_ERR_ARGUMENT, "drop: negative iteration count");
     const int nv = c->geo.num_voxels;
     if (!c->diag_ready) {
-        if (c->cfg.drop_form == PCT_DROP_SCATTER) PCT_TRY(build_scatter(c));
-        else PCT_TRY(build_aggregated(c));
         pct_drop_release_graph(c);
+        c->td.release();
+        const int form = c->cfg.drop_form;
+        if (form == PCT_DROP_TILED && pct_drop_tiled_fits(c)) {
+            PCT_TRY(pct_drop_tiled_build(c));
+            const int64_t B = c->cfg.block_size;
+            c->num_blocks = c->td.num_blocks;
+            c->drop_mode = PCT_DROP_TILED;
+            c->drop_launches_per_iter = 0;
+            for (int b = 0; b < c->num_blocks; ++b)
+                c->drop_launches_per_iter += 2 + (c->td.fw_base[b + 1] > c->td.fw_base[b] ? 1 : 0);
+            (void)B;
+            c->diag_ready = 1;
+        } else if (form == PCT_DROP_SORTED) {
+            PCT_TRY(build_sorted(c));
+        } else {
+            PCT_TRY(build_scatter(c));
+        }
     }
     PCT_TRY(c->x_update.alloc(sizeof(float) * nv));
     PCT_CUDA(cudaMemsetAsync(c->x_update.p, 0, sizeof(float) * nv, c->stream));
@@ -511,7 +343,7 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
     double res_host[maxit + 2];
     for (int it = 0; it < iterations; ++it) {
         PCT_CUDA(cudaGraphLaunch(c->drop_graph_exec, c->stream));
-        c->launches += 2 * (int64_t)c->num_blocks;
+        c->launches += c->drop_launches_per_iter;
         ++c->launches;
         k_store_resid<<<1, 1, 0, c->stream>>>(d_res + maxit, d_res + (it < maxit ? it : maxit - 1));
         ++done;

@@ -246,7 +246,7 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     int e = pct_geometry_derive(cfg, &g);
     if (e) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: invalid geometry (code %d)", e);
     if (cfg->block_size <= 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: block_size must be positive");
-    if (cfg->drop_form < 0 || cfg->drop_form > PCT_DROP_SCATTER)
+    if (cfg->drop_form < PCT_DROP_SCATTER || cfg->drop_form > PCT_DROP_TILED)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_form %d", cfg->drop_form);
     if (cfg->mlp_hull < 0 || cfg->mlp_hull > 3) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: bad mlp_hull");
     int ndev = 0;
@@ -290,6 +290,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows,
                      &c->drop_perm, &c->drop_sort};
     for (DevBuf* b : all) b->release();
+    c->td.release();
     for (auto& b : c->in13) b.release();
     pct_drop_release_graph(c);
     c->h.release();

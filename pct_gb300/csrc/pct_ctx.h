@@ -20,6 +20,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 #include <cstddef>
 #include "pct_internal.h"
 
@@ -81,6 +82,26 @@ enum Stage {
     ST_EMPTY = 0, ST_BINNED, ST_HULLS_DONE, ST_CUT, ST_FBP, ST_HULL_SELECTED, ST_X0, ST_ENDPOINTS, ST_ROWS
 };
 
+/* Rows regrouped per (DROP block, image tile) for the tiled DROP form. */
+struct TiledDrop {
+    DevBuf row_seg_off, row_nseg, bt_cnt, seg_bt, ent_bt, seg_base, ent_base, work;
+    DevBuf seg_row, seg_slot, seg_ent, partial, ent, u, umax, smax, counts, cursor, seg_sub, ent_sub;
+    std::vector<int> fw_base;  /* forward work items of each block: [fw_base[b], fw_base[b + 1]) */
+    int num_blocks = 0;
+    DevBuf* all[20] = {&row_seg_off, &row_nseg, &bt_cnt, &seg_bt, &ent_bt, &seg_base, &ent_base, &work, &seg_row,
+                       &seg_slot, &seg_ent, &partial, &ent, &u, &umax, &smax, &counts, &cursor, &seg_sub, &ent_sub};
+    size_t bytes_held() const {
+        size_t t = 0;
+        for (DevBuf* b : all) t += b->bytes;
+        return t;
+    }
+    void release() {
+        for (DevBuf* b : all) b->release();
+        fw_base.clear();
+        num_blocks = 0;
+    }
+};
+
 struct pct_ctx {
     pct_config cfg;
     pct_geometry geo;
@@ -120,7 +141,9 @@ struct pct_ctx {
     int64_t row_capacity = 0;
     int num_blocks = 0;
     int diag_ready = 0;
-    int drop_aggregated = 0;       /* DROP runs in the aggregated form (else scatter) */
+    int drop_mode = 0;             /* built DROP form: PCT_DROP_TILED / _SORTED / _SCATTER */
+    int drop_launches_per_iter = 0;
+    TiledDrop td;
 
     pct_status set_device() {
         cudaError_t e = cudaSetDevice(device);
@@ -149,11 +172,15 @@ pct_status pct_compact_histories(pct_ctx* c, const uint8_t* d_keep, int64_t n, i
 
 /* Device error counters (indices into err_flags, uint64). */
 enum { ERR_WALK_CAPPED = 0, ERR_VOXEL_OUTSIDE = 1, ERR_FIXED_OVERFLOW = 2, ERR_ROW_OVERFLOW = 3,
-       ERR_MLP_FP64 = 4, ERR_ROWS_OUTSIDE = 5, ERR_MLP_QUEUED = 6, ERR_MLP_FIXROWS = 7, ERR_COUNT = 8 };
+       ERR_MLP_FP64 = 4, ERR_ROWS_OUTSIDE = 5, ERR_MLP_QUEUED = 6, ERR_MLP_FIXROWS = 7, ERR_DROP_NONFINITE = 8,
+       ERR_COUNT = 16 };
 
 DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g);
 void pct_drop_release_graph(pct_ctx* c);
 pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* off, int64_t* total);
 pct_status pct_rows_dense(pct_ctx* c, int64_t* total, DevBuf* dense_off, DevBuf* dense);
+int pct_drop_tiled_fits(pct_ctx* c);
+pct_status pct_drop_tiled_build(pct_ctx* c);
+void pct_drop_tiled_enqueue(pct_ctx* c, int block, double* resid);
 
 #endif

@@ -100,7 +100,7 @@ PCT_GFN void pct_config_fill_defaults(pct_config* c) {
     c->chord_bf16 = 0;
     c->mlp_exact = 0;
     c->mlp_face_margin = 2e-5;
-    c->drop_form = PCT_DROP_AGGREGATED;
+    c->drop_form = PCT_DROP_SCATTER;
 }
 
 /* Returns 0 on success, nonzero when a derived size is out of range. */

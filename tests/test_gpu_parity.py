@@ -175,9 +175,10 @@ def test_drop_within_tolerance_of_fp64(run):
     assert all(np.isfinite(st.residual[k]) and st.residual[k] > 0 for k in range(its))
 
 
-def test_drop_scatter_form_within_tolerance(run):
-    """The atomic scatter form of the DROP block step (the fallback when the
-    transposed copy does not fit) against the same binary64 iterate."""
+@pytest.mark.parametrize("form", [1, 2])
+def test_drop_other_forms_within_tolerance(run, form):
+    """The sorted (1) and tiled (2) forms of the DROP block step against the
+    same binary64 iterate (the default scatter form is checked above)."""
     name, cfg, ora, out = run
     its = cfg.iterations
     if its == 0:
@@ -185,7 +186,7 @@ def test_drop_scatter_form_within_tolerance(run):
     cfg2 = phantoms.make_config({})
     for f, _ in cfg._fields_:
         setattr(cfg2, f, getattr(cfg, f))
-    cfg2.drop_form = 2
+    cfg2.drop_form = form
     w, _ = CASES[name]()
     data, angles = phantoms.generate(w)
     r = recon.run_full(cfg2, data, angles)
@@ -197,3 +198,31 @@ def test_drop_scatter_form_within_tolerance(run):
     ref = ora["x_%d" % its]
     err = np.linalg.norm(x - ref) / np.linalg.norm(ref)
     assert err <= DROP_TOL, "relative L2 %.3e" % err
+
+
+def test_drop_tiled_form_is_reproducible(run):
+    """The tiled form accumulates the dots and the block updates in integers:
+    repeating the same iterations, in this context or a new one, gives the
+    same image bit for bit."""
+    name, cfg, ora, out = run
+    its = cfg.iterations
+    if its == 0:
+        pytest.skip("no iterations")
+    cfg2 = phantoms.make_config({})
+    for f, _ in cfg._fields_:
+        setattr(cfg2, f, getattr(cfg, f))
+    cfg2.drop_form = 2
+    w, over = CASES[name]()
+    data, angles = phantoms.generate(w)
+    images = []
+    for rep in range(2):
+        r = recon.run_full(cfg2, data, angles)
+        r.collect_mlp_endpoints()
+        r.mlp_rows()
+        for _ in range(2 - rep):
+            r.reset_iterate()
+            r.drop(its)
+            images.append(r.array("X"))
+        r.close()
+    assert same(images[0], images[1])
+    assert same(images[0], images[2])
