@@ -98,6 +98,7 @@ typedef struct pct_config {
     double mlp_face_margin;        /* [cm] binary32 MLP samples closer than this to a voxel face
                                       are recomputed in binary64 (default 2e-5) */
     int drop_form;                 /* DROP block step: PCT_DROP_SCATTER (default), _SORTED or _TILED */
+    int walk_exact;                /* 1: every hull-walk step in binary64 (slow path, for checks) */
 } pct_config;
 
 /* DROP block step forms; all compute the same block update.  SCATTER adds
@@ -170,6 +171,7 @@ typedef struct pct_counts {
     int64_t rows_outside_image;      /* row entries whose voxel index lies outside the image */
     int64_t walks_capped;            /* hull/endpoint walks stopped by the step cap */
     int64_t mlp_fp64_samples;        /* MLP samples recomputed in FP64 near a voxel face */
+    int64_t walk_fp64_steps;         /* hull-walk steps taken in FP64 (binary32 could not certify them) */
     int64_t kernel_launches;         /* kernels this context has launched (graph nodes included) */
 } pct_counts;
 

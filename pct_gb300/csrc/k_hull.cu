@@ -5,7 +5,8 @@
  *   k_hull_walk      SC_GPU / MSC_GPU / SM_GPU (.cu:3338-3710): straight-line
  *                    voxel walk from the cylinder entry to the exit voxel with
  *                    take_2D_step_GPU / take_3D_step_GPU (.cu:8754-8866), binary64
- *                    in source order, one thread per history.  The reference
+ *                    in source order, one thread per history (walk_exact).
+ *   k_hull_walk_fast the same walk with certified binary32 steps (default).  The reference
  *                    walk has no bound (a walk that passes its exit voxel heading
  *                    to negative indices never ends and writes out of bounds);
  *                    here it stops after 4 (C + R + S) + 16 steps and voxels
@@ -153,6 +154,298 @@ __global__ void __launch_bounds__(256) k_hull_walk(DevGeom g, int kind, double t
     }
 }
 
+/* ---- binary32 walk with certified decisions ------------------------------------
+ * The state after a walk step is a function of the axis crossed and the voxel
+ * indices right after that crossing: step2/step3 recompute every coordinate
+ * and distance from the crossed edge (nothing accumulates).  k_hull_walk_fast
+ * keeps the state in binary32 together with a bound on its distance from the
+ * binary64 state, takes a step in binary32 only when every comparison that
+ * decides it (and every exact-zero distance test after it) is certain under
+ * those bounds, and otherwise rebuilds the binary64 state from the last
+ * crossing and takes the step with step2/step3.  The voxel sequence is that
+ * of the binary64 walk. */
+enum { AX_NONE = 0, AX_X = 1, AX_Y = 2, AX_Z = 3 };
+constexpr float WU = 1.2e-7f; /* twice the binary32 unit roundoff */
+
+struct WalkLine {
+    double xs, ys, zs;
+    double dy_dx, dz_dx, dz_dy, dx_dy, dx_dz, dy_dz;
+    int xm, ym, zm;
+};
+
+/* Binary64 state after crossing axis a with indices (ax, ay, az) before the
+ * zero-distance adjustments (AX_NONE: the start of the walk). */
+__device__ __noinline__ void walk_state64(const DevGeom& g, const WalkLine& L, int a, int ax, int ay, int az, Walk& w,
+                                          double z_init, double z_to_go_init) {
+    w.vx = ax;
+    w.vy = ay;
+    w.vz = az;
+    const bool is3d = L.zm != 0;
+    if (a == AX_NONE) {
+        w.x = L.xs;
+        w.y = L.ys;
+        w.z = L.zs;
+        w.x_to_go = dev_distance_remaining(g.x_zero, w.x, PCT_X_INC, L.xm, g.voxel_width, w.vx);
+        w.y_to_go = dev_distance_remaining(g.y_zero, w.y, PCT_Y_INC, L.ym, g.voxel_height, w.vy);
+        w.z_to_go = dev_distance_remaining(g.z_zero, w.z, PCT_Z_INC, L.zm, g.voxel_thickness, w.vz);
+    } else {
+        if (a == AX_X) {
+            w.x = dev_edge_coordinate(g.x_zero, w.vx, g.voxel_width, PCT_X_INC, L.xm);
+            w.y = dev_corresponding(L.dy_dx, w.x, L.xs, L.ys);
+            w.x_to_go = g.voxel_width;
+            w.y_to_go = dev_distance_remaining(g.y_zero, w.y, PCT_Y_INC, L.ym, g.voxel_height, w.vy);
+            if (is3d) {
+                w.z = dev_corresponding(L.dz_dx, w.x, L.xs, L.zs);
+                w.z_to_go = dev_distance_remaining(g.z_zero, w.z, PCT_Z_INC, L.zm, g.voxel_thickness, w.vz);
+            }
+        } else if (a == AX_Y) {
+            w.y = dev_edge_coordinate(g.y_zero, w.vy, g.voxel_height, PCT_Y_INC, L.ym);
+            w.x = dev_corresponding(L.dx_dy, w.y, L.ys, L.xs);
+            w.x_to_go = dev_distance_remaining(g.x_zero, w.x, PCT_X_INC, L.xm, g.voxel_width, w.vx);
+            w.y_to_go = g.voxel_height;
+            if (is3d) {
+                w.z = dev_corresponding(L.dz_dy, w.y, L.ys, L.zs);
+                w.z_to_go = dev_distance_remaining(g.z_zero, w.z, PCT_Z_INC, L.zm, g.voxel_thickness, w.vz);
+            }
+        } else {
+            w.z = dev_edge_coordinate(g.z_zero, w.vz, g.voxel_thickness, PCT_Z_INC, L.zm);
+            w.x = dev_corresponding(L.dx_dz, w.z, L.zs, L.xs);
+            w.y = dev_corresponding(L.dy_dz, w.z, L.zs, L.ys);
+            w.x_to_go = dev_distance_remaining(g.x_zero, w.x, PCT_X_INC, L.xm, g.voxel_width, w.vx);
+            w.y_to_go = dev_distance_remaining(g.y_zero, w.y, PCT_Y_INC, L.ym, g.voxel_height, w.vy);
+            w.z_to_go = g.voxel_thickness;
+        }
+        if (!is3d) {
+            w.z = z_init;
+            w.z_to_go = z_to_go_init;
+        }
+        if (w.x_to_go == 0) { w.x_to_go = g.voxel_width; w.vx += L.xm; }
+        if (w.y_to_go == 0) { w.y_to_go = g.voxel_height; w.vy -= L.ym; }
+        if (is3d && w.z_to_go == 0) { w.z_to_go = g.voxel_thickness; w.vz -= L.zm; }
+        if (w.vz < 0) w.vz = 0;
+    }
+    w.voxel = w.vx + w.vy * g.columns + w.vz * g.columns * g.rows;
+}
+
+/* binary32 state with error bounds */
+struct Walk32 {
+    float x, y, z, xt, yt, zt;      /* coordinates and distances to the next edges */
+    float ex, ey, ez, ext, eyt, ezt; /* bounds on |binary32 - binary64| */
+};
+
+__device__ __forceinline__ void walk_to32(const Walk& w, Walk32& f) {
+    f.x = (float)w.x; f.y = (float)w.y; f.z = (float)w.z;
+    f.xt = (float)w.x_to_go; f.yt = (float)w.y_to_go; f.zt = (float)w.z_to_go;
+    f.ex = WU * fabsf(f.x); f.ey = WU * fabsf(f.y); f.ez = WU * fabsf(f.z);
+    f.ext = WU * f.xt; f.eyt = WU * f.yt; f.ezt = WU * f.zt;
+}
+
+/* edge_coordinate_GPU in binary32 and a bound on its error */
+__device__ __forceinline__ float edge32(float zero, int voxel_entered, float size, int inc, int step, float* err) {
+    int on_edge = (step == inc) ? voxel_entered : voxel_entered + 1;
+    float k = (float)(inc * on_edge);
+    float prod = k * size;
+    float e = zero + prod;
+    *err = WU * (fabsf(zero) + 2.0f * fabsf(prod) + fabsf(e));
+    return e;
+}
+
+/* corresponding_coordinate in binary32: m (p - p0) + q0 with |error of p| <= ep */
+__device__ __forceinline__ float corr32(float m, float p, float p0, float q0, float ep, float* err) {
+    float d = p - p0;
+    float md = m * d;
+    float r = md + q0;
+    *err = fabsf(m) * (ep + WU * fabsf(d)) + WU * (fabsf(md) + fabsf(r));
+    return r;
+}
+
+/* a <= b decided with certainty: 1 / 0, or -1 when the bounds overlap */
+__device__ __forceinline__ int cmp_le(float a, float ea, float b, float eb) {
+    float d = b - a;
+    float tol = ea + eb + WU * (fabsf(a) + fabsf(b));
+    if (d > tol) return 1;
+    if (-d > tol) return 0;
+    return -1;
+}
+
+/* One walk step in binary32; returns false (state untouched) when a decision is uncertain. */
+__device__ __forceinline__ bool step32(const DevGeom& g, const WalkLine& L, const float* m32, Walk32& f, int& vx,
+                                       int& vy, int& vz, int& a_axis, int& ax, int& ay, int& az) {
+    const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
+    const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
+    const float xs = (float)L.xs, ys = (float)L.ys, zs = (float)L.zs;
+    /* m32: dy_dx, dz_dx, dz_dy, dx_dy, dx_dz, dy_dz */
+    int axis;
+    if (L.zm != 0) {
+        float x_ext = fabsf(m32[1]) * f.xt, e_xext = fabsf(m32[1]) * f.ext + WU * x_ext;
+        float y_ext = fabsf(m32[2]) * f.yt, e_yext = fabsf(m32[2]) * f.eyt + WU * y_ext;
+        int c1 = cmp_le(f.zt, f.ezt, x_ext, e_xext);
+        int c2 = cmp_le(f.zt, f.ezt, y_ext, e_yext);
+        if (c1 < 0 || c2 < 0) return false;
+        if (c1 && c2) {
+            axis = AX_Z;
+        } else {
+            int c3 = cmp_le(x_ext, e_xext, y_ext, e_yext);
+            if (c3 < 0) return false;
+            axis = c3 ? AX_X : AX_Y;
+        }
+    } else {
+        float y_ext = fabsf(m32[3]) * f.yt, e_yext = fabsf(m32[3]) * f.eyt + WU * y_ext;
+        int c = cmp_le(f.xt, f.ext, y_ext, e_yext);
+        if (c < 0) return false;
+        axis = c ? AX_X : AX_Y;
+    }
+    int nx = vx, ny = vy, nz = vz;
+    Walk32 n = f;
+    float e_edge;
+    if (axis == AX_X) {
+        nx += L.xm;
+        n.x = edge32(X0, nx, VW, PCT_X_INC, L.xm, &n.ex);
+        n.y = corr32(m32[0], n.x, xs, ys, n.ex, &n.ey);
+        n.xt = VW;
+        n.ext = WU * VW;
+        float ey_edge = 0.0f;
+        float ye = edge32(Y0, ny + PCT_Y_INC * L.ym, VH, PCT_Y_INC, L.ym, &ey_edge);
+        n.yt = fabsf(ye - n.y);
+        n.eyt = ey_edge + n.ey + WU * n.yt;
+        if (L.zm != 0) {
+            n.z = corr32(m32[1], n.x, xs, zs, n.ex, &n.ez);
+            float ze = edge32(Z0, nz + PCT_Z_INC * L.zm, VT, PCT_Z_INC, L.zm, &e_edge);
+            n.zt = fabsf(ze - n.z);
+            n.ezt = e_edge + n.ez + WU * n.zt;
+        }
+    } else if (axis == AX_Y) {
+        ny -= L.ym;
+        n.y = edge32(Y0, ny, VH, PCT_Y_INC, L.ym, &n.ey);
+        n.x = corr32(m32[3], n.y, ys, xs, n.ey, &n.ex);
+        float xe = edge32(X0, nx + PCT_X_INC * L.xm, VW, PCT_X_INC, L.xm, &e_edge);
+        n.xt = fabsf(xe - n.x);
+        n.ext = e_edge + n.ex + WU * n.xt;
+        n.yt = VH;
+        n.eyt = WU * VH;
+        if (L.zm != 0) {
+            n.z = corr32(m32[2], n.y, ys, zs, n.ey, &n.ez);
+            float ze = edge32(Z0, nz + PCT_Z_INC * L.zm, VT, PCT_Z_INC, L.zm, &e_edge);
+            n.zt = fabsf(ze - n.z);
+            n.ezt = e_edge + n.ez + WU * n.zt;
+        }
+    } else {
+        nz -= L.zm;
+        n.z = edge32(Z0, nz, VT, PCT_Z_INC, L.zm, &n.ez);
+        n.x = corr32(m32[4], n.z, zs, xs, n.ez, &n.ex);
+        n.y = corr32(m32[5], n.z, zs, ys, n.ez, &n.ey);
+        float xe = edge32(X0, nx + PCT_X_INC * L.xm, VW, PCT_X_INC, L.xm, &e_edge);
+        n.xt = fabsf(xe - n.x);
+        n.ext = e_edge + n.ex + WU * n.xt;
+        float ye = edge32(Y0, ny + PCT_Y_INC * L.ym, VH, PCT_Y_INC, L.ym, &e_edge);
+        n.yt = fabsf(ye - n.y);
+        n.eyt = e_edge + n.ey + WU * n.yt;
+        n.zt = VT;
+        n.ezt = WU * VT;
+    }
+    /* the exact-zero distance tests must be certain too */
+    if (n.xt <= n.ext || n.yt <= n.eyt || (L.zm != 0 && n.zt <= n.ezt)) return false;
+    if (!(n.ext < 1e-3f && n.eyt < 1e-3f && n.ezt < 1e-3f)) return false; /* bounds out of their useful range */
+    a_axis = axis;
+    ax = nx;
+    ay = ny;
+    az = nz;
+    if (nz < 0) nz = 0;
+    vx = nx;
+    vy = ny;
+    vz = nz;
+    f = n;
+    return true;
+}
+
+/* Same walk and image updates as k_hull_walk. */
+__global__ void __launch_bounds__(256) k_hull_walk_fast(DevGeom g, int kind, double threshold, int64_t n,
+                                                        const uint8_t* __restrict__ missed, HistView h,
+                                                        int* __restrict__ img, unsigned long long* __restrict__ flags) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float wepl = h.wepl[i];
+    int use = kind == 2 ? (wepl >= threshold) : (wepl <= threshold);
+    if (missed[i] || !use) return;
+    const float xe = h.x_entry[i], ye = h.y_entry[i], ze = h.z_entry[i];
+    const float xx = h.x_exit[i], yx = h.y_exit[i], zx = h.z_exit[i];
+    WalkLine L;
+    L.xm = (xe <= xx) - (xe >= xx);
+    L.ym = (ye <= yx) - (ye >= yx);
+    L.zm = (ze <= zx) - (ze >= zx);
+    L.xs = xe; L.ys = ye; L.zs = ze;
+    float m32[6];
+    m32[0] = (yx - ye) / (xx - xe);
+    m32[1] = (zx - ze) / (xx - xe);
+    m32[2] = (zx - ze) / (yx - ye);
+    m32[3] = (xx - xe) / (yx - ye);
+    m32[4] = (xx - xe) / (zx - ze);
+    m32[5] = (yx - ye) / (zx - ze);
+    L.dy_dx = m32[0]; L.dz_dx = m32[1]; L.dz_dy = m32[2]; L.dx_dy = m32[3]; L.dx_dz = m32[4]; L.dy_dz = m32[5];
+    Walk w;
+    walk_state64(g, L, AX_NONE, dev_calculate_voxel(g.x_zero, xe, g.voxel_width),
+                 dev_calculate_voxel(g.y_zero, ye, g.voxel_height), dev_calculate_voxel(g.z_zero, ze, g.voxel_thickness),
+                 w, 0.0, 0.0);
+    const double z_init = w.z, zt_init = w.z_to_go;
+    Walk32 f;
+    walk_to32(w, f);
+    int vx = w.vx, vy = w.vy, vz = w.vz;
+    int a_axis = AX_NONE, ax = vx, ay = vy, az = vz;
+    int vxo = dev_calculate_voxel(g.x_zero, xx, g.voxel_width);
+    int vyo = dev_calculate_voxel(g.y_zero, yx, g.voxel_height);
+    int vzo = dev_calculate_voxel(g.z_zero, zx, g.voxel_thickness);
+    int voxel_out = vxo + vyo * g.columns + vzo * g.columns * g.rows;
+    int voxel = vx + vy * g.columns + vz * g.columns * g.rows;
+    int end = (voxel == voxel_out) || (vx >= g.columns) || (vy >= g.rows) || (vz >= g.slices);
+    const int cap = 4 * (g.columns + g.rows + g.slices) + 16;
+    int steps = 0;
+    unsigned long long exact_steps = 0;
+    for (;;) {
+        if (!end) {
+            if (voxel >= 0 && voxel < g.num_voxels) {
+                if (kind == 0) img[voxel] = 0;
+                else atomicAdd(img + voxel, 1);
+            } else {
+                dev_flag(flags, ERR_VOXEL_OUTSIDE);
+            }
+        }
+        if (end) break;
+        if (++steps > cap) {
+            dev_flag(flags, ERR_WALK_CAPPED);
+            break;
+        }
+        if (!step32(g, L, m32, f, vx, vy, vz, a_axis, ax, ay, az)) {
+            /* binary64 step from the binary64 state of the last crossing */
+            walk_state64(g, L, a_axis, ax, ay, az, w, z_init, zt_init);
+            int bx = w.vx, by = w.vy, bz = w.vz;
+            int axis;
+            if (L.zm != 0) {
+                double x_ext = fabs(L.dz_dx) * w.x_to_go, y_ext = fabs(L.dz_dy) * w.y_to_go;
+                if ((w.z_to_go <= x_ext) && (w.z_to_go <= y_ext)) axis = AX_Z;
+                else axis = x_ext <= y_ext ? AX_X : AX_Y;
+            } else {
+                axis = w.x_to_go <= fabs(L.dx_dy) * w.y_to_go ? AX_X : AX_Y;
+            }
+            if (axis == AX_X) bx += L.xm;
+            else if (axis == AX_Y) by -= L.ym;
+            else bz -= L.zm;
+            a_axis = axis;
+            ax = bx;
+            ay = by;
+            az = bz;
+            walk_state64(g, L, a_axis, ax, ay, az, w, z_init, zt_init);
+            walk_to32(w, f);
+            vx = w.vx;
+            vy = w.vy;
+            vz = w.vz;
+            ++exact_steps;
+        }
+        voxel = vx + vy * g.columns + vz * g.columns * g.rows;
+        end = (voxel == voxel_out) || (vx >= g.columns) || (vy >= g.rows) || (vz >= g.slices);
+    }
+    if (exact_steps) atomicAdd(flags + ERR_WALK_FP64, exact_steps);
+}
+
 __device__ __forceinline__ int dev_outside_rim(const DevGeom& g, int c, int r) {
     float x = (float)((c - g.columns / 2 + 0.5) * g.voxel_width);
     float y = (float)((g.rows / 2 - r - 0.5) * g.voxel_height);
@@ -279,17 +572,23 @@ pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed) {
     HistView h = c->view(c->h2);
     unsigned grid = pct_grid_for(n, 256);
     unsigned long long* flags = c->err_flags.as<unsigned long long>();
+    const bool exact = c->cfg.walk_exact != 0;
+    auto walk = [&](const DevGeom& g, int kind, double thr, int64_t nn, const uint8_t* ms, const HistView& hv, int* img,
+                    unsigned long long* fl) {
+        if (exact) k_hull_walk<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, img, fl);
+        else k_hull_walk_fast<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, img, fl);
+    };
     if (c->cfg.sc_on) {
         ++c->launches;
-        k_hull_walk<<<grid, 256, 0, c->stream>>>(c->dg, 0, c->cfg.sc_threshold, n, missed, h, c->sc_hull.as<int>(), flags);
+        walk(c->dg, 0, c->cfg.sc_threshold, n, missed, h, c->sc_hull.as<int>(), flags);
     }
     if (c->cfg.msc_on) {
         ++c->launches;
-        k_hull_walk<<<grid, 256, 0, c->stream>>>(c->dg, 1, c->cfg.msc_threshold, n, missed, h, c->msc_counts.as<int>(), flags);
+        walk(c->dg, 1, c->cfg.msc_threshold, n, missed, h, c->msc_counts.as<int>(), flags);
     }
     if (c->cfg.sm_on) {
         ++c->launches;
-        k_hull_walk<<<grid, 256, 0, c->stream>>>(c->dg, 2, c->cfg.sm_lower_threshold, n, missed, h, c->sm_counts.as<int>(), flags);
+        walk(c->dg, 2, c->cfg.sm_lower_threshold, n, missed, h, c->sm_counts.as<int>(), flags);
     }
     PCT_CUDA(cudaGetLastError());
     return PCT_OK;

@@ -325,6 +325,7 @@ extern "C" pct_status pct_get_counts(pct_ctx* c, pct_counts* out) {
     }
     out->walks_capped = (int64_t)f[ERR_WALK_CAPPED];
     out->mlp_fp64_samples = (int64_t)f[ERR_MLP_FP64];
+    out->walk_fp64_steps = (int64_t)f[ERR_WALK_FP64];
     out->rows_outside_image = (int64_t)f[ERR_ROWS_OUTSIDE];
     out->kernel_launches = c->launches;
     return PCT_OK;

@@ -173,7 +173,7 @@ pct_status pct_compact_histories(pct_ctx* c, const uint8_t* d_keep, int64_t n, i
 /* Device error counters (indices into err_flags, uint64). */
 enum { ERR_WALK_CAPPED = 0, ERR_VOXEL_OUTSIDE = 1, ERR_FIXED_OVERFLOW = 2, ERR_ROW_OVERFLOW = 3,
        ERR_MLP_FP64 = 4, ERR_ROWS_OUTSIDE = 5, ERR_MLP_QUEUED = 6, ERR_MLP_FIXROWS = 7, ERR_DROP_NONFINITE = 8,
-       ERR_COUNT = 16 };
+       ERR_WALK_FP64 = 9, ERR_COUNT = 16 };
 
 DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g);
 void pct_drop_release_graph(pct_ctx* c);

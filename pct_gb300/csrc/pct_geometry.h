@@ -101,6 +101,7 @@ PCT_GFN void pct_config_fill_defaults(pct_config* c) {
     c->mlp_exact = 0;
     c->mlp_face_margin = 2e-5;
     c->drop_form = PCT_DROP_SCATTER;
+    c->walk_exact = 0;
 }
 
 /* Returns 0 on success, nonzero when a derived size is out of range. */
