@@ -274,11 +274,22 @@ pct_status pct_drop_noalloc(int64_t n, const int64_t* row_offsets, const uint32_
                             const float* wepl, int num_voxels, int block_size, float lambda, int iterations,
                             float* x, double* residual_sq, void* stream);
 
+/* PCTD version-0 files (count_histories_v0 .cu:997-1097, read_data_chunk_v02
+ * .cu:1769-1933): header query, read into 13 caller host arrays of at least
+ * `capacity` floats (t0..t3, v0..v3, u0..u3, WEPL in mm), write, and
+ * read+upload of whole files as chunks (one file per gantry angle). */
+pct_status pct_pctd_info(const char* path, int64_t* num_histories, float* projection_angle, float* beam_energy);
+pct_status pct_pctd_read(const char* path, float* const data13[13], int64_t capacity, int64_t* num_histories,
+                         float* projection_angle);
+pct_status pct_pctd_write(const char* path, const float* const data13[13], int64_t num_histories,
+                          float projection_angle, float beam_energy);
+pct_status pct_process_pctd_files(pct_ctx* ctx, const char* const* paths, int num_files);
+
 pct_status pct_config_default(pct_config* cfg);
 pct_status pct_geometry_from_config(const pct_config* cfg, pct_geometry* geo);
 const char* pct_last_error(void);
 const char* pct_status_string(pct_status s);
-/* sizeof of ABI structs (0 config, 1 geometry, 2 phantom object, 3 scan params, ...). */
+/* sizeof of ABI structs (0 config, 1 geometry, 2 phantom object, 3 scan params, 4 counts, 5 drop stats). */
 size_t pct_sizeof(int which);
 
 #ifdef __cplusplus

@@ -23,6 +23,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libpct_gb300.so")
+COMPAT_SRC = os.path.join(PKG, "compat", "pct_functions_compat.cpp")
+COMPAT_LIB = os.path.join(LIBDIR, "libpct_compat.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
@@ -85,7 +87,22 @@ def build(verbose=False, extra=None):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr + r.stdout)
+    build_compat()
     return LIB
+
+
+def build_compat():
+    """libpct_compat.so: the reference's entry-point names over the C ABI (host C++ only)."""
+    if (os.path.exists(COMPAT_LIB) and os.path.getmtime(COMPAT_LIB) >= os.path.getmtime(LIB)
+            and os.path.getmtime(COMPAT_LIB) >= os.path.getmtime(COMPAT_SRC)):
+        return COMPAT_LIB
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), COMPAT_SRC,
+           "-L", LIBDIR, "-lpct_gb300", "-Wl,-rpath,$ORIGIN", "-o", COMPAT_LIB]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("compat link failed:\n" + r.stderr + r.stdout)
+    return COMPAT_LIB
 
 
 if __name__ == "__main__":

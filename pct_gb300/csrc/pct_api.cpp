@@ -52,6 +52,8 @@ extern "C" size_t pct_sizeof(int which) {
         case 1: return sizeof(pct_geometry);
         case 2: return sizeof(pct_phantom_object);
         case 3: return sizeof(pct_scan_params);
+        case 4: return sizeof(pct_counts);
+        case 5: return sizeof(pct_drop_stats);
     }
     return 0;
 }

@@ -68,6 +68,7 @@ def _declare(lib):
     lib.pct_reset_iterate.argtypes = [vp]
     lib.pct_stream.restype = vp
     lib.pct_stream.argtypes = [vp]
+    lib.pct_process_pctd_files.argtypes = [vp, C.POINTER(C.c_char_p), ci]
 
 
 class Reconstruction:
@@ -112,6 +113,11 @@ class Reconstruction:
         n = data13.shape[1]
         ptrs = (C.c_void_p * 13)(*[data13[k].ctypes.data for k in range(13)])
         self._call("pct_process_chunk", ptrs, projection_angle.ctypes.data, n, 0)
+
+    def process_pctd_files(self, paths):
+        """Reads PCTD v0 files (one per gantry angle) and uploads each as a chunk."""
+        arr = (C.c_char_p * len(paths))(*[p.encode() for p in paths])
+        self._call("pct_process_pctd_files", arr, len(paths))
 
     def process_chunk_device(self, ptrs13, angle_ptr, n):
         """Device pointers (ints) to the 13 PCTD arrays and the angles."""
