@@ -280,10 +280,10 @@ def main():
     traffic = None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
-        t = tr.get("drop_form_%d" % a.drop_form)
-        if t:  # DRAM bytes of one iteration, scaled from a smaller ncu capture
+        tm = tr.get("drop_form_%d" % a.drop_form)
+        if tm:  # DRAM bytes of one iteration, scaled from a smaller ncu capture
             nblocks = (R + cfg.block_size - 1) // cfg.block_size
-            traffic = t["ratio_to_algorithmic"] * drop_bytes + t["per_block_bytes"] * nblocks
+            traffic = tm["ratio_to_algorithmic"] * drop_bytes + tm["per_block_bytes"] * nblocks
     except Exception:
         pass
 

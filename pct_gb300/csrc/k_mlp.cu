@@ -474,9 +474,11 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
                                                   uint32_t* __restrict__ rows, int* __restrict__ row_len,
                                                   MlpDeferred* __restrict__ queue, int64_t queue_cap,
                                                   int64_t* __restrict__ fix_rows,
-                                                  unsigned long long* __restrict__ flags) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                                                  unsigned long long* __restrict__ flags,
+                                                  const uint32_t* __restrict__ order) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int64_t i = order ? (int64_t)order[t] : t;
     const MlpRec& R = rec[i];
     const double u_2 = R.m.u_2;
     const int K = dev_sample_count(tab, kmax, u_2, g.mlp_u_step);
@@ -556,11 +558,64 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
     row_len[i] = len;
     if (deferred) {
         unsigned long long r = atomicAdd(flags + ERR_MLP_FIXROWS, 1ull);
-        fix_rows[r] = i; /* r < number of queued samples <= queue_cap */
+        fix_rows[r] = i; /* at most one entry per row: r < n */
     } else if (outside) {
         atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
     }
     if (fp64_samples) atomicAdd(flags + ERR_MLP_FP64, (unsigned long long)fp64_samples);
+}
+
+/* Histories in decreasing order of sample count, so that the 32 rows of a
+ * warp of k_mlp_fast have nearly the same length (a counting sort by the slot
+ * size bound[i] = K_i + 1; the order within one count does not matter). */
+__global__ void k_kcount(int64_t n, const int64_t* __restrict__ bound, int nkeys, unsigned* __restrict__ cnt) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t b = bound[i];
+    int key = b < nkeys ? (int)(nkeys - 1 - b) : 0; /* decreasing */
+    atomicAdd(cnt + key, 1u);
+}
+
+/* exclusive scan of nkeys counts in one CTA (nkeys is a few thousand) */
+__global__ void k_kscan(int nkeys, unsigned* __restrict__ cnt) {
+    __shared__ unsigned ws[32];
+    __shared__ unsigned carry_s;
+    if (threadIdx.x == 0) carry_s = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int base = 0; base < nkeys; base += blockDim.x) {
+        int k = base + threadIdx.x;
+        unsigned v = k < nkeys ? cnt[k] : 0u, x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            unsigned t = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            ws[lane] = t;
+        }
+        __syncthreads();
+        unsigned incl = x + (w > 0 ? ws[w - 1] : 0u);
+        if (k < nkeys) cnt[k] = carry_s + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry_s += incl;
+        __syncthreads();
+    }
+}
+
+__global__ void k_kplace(int64_t n, const int64_t* __restrict__ bound, int nkeys, unsigned* __restrict__ cursor,
+                         uint32_t* __restrict__ order) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t b = bound[i];
+    int key = b < nkeys ? (int)(nkeys - 1 - b) : 0;
+    order[atomicAdd(cursor + key, 1u)] = (uint32_t)i;
 }
 
 /* The queued samples in binary64, one thread each. */
@@ -579,11 +634,11 @@ __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __rest
 }
 
 /* Drops consecutive repeats in the rows that had queued samples. */
-__global__ void k_mlp_dedupe(int64_t queue_cap, const int64_t* __restrict__ fix_rows,
+__global__ void k_mlp_dedupe(int64_t rows_cap, const int64_t* __restrict__ fix_rows,
                              const int64_t* __restrict__ row_start, int* __restrict__ row_len,
                              uint32_t* __restrict__ rows, uint32_t nv, unsigned long long* __restrict__ flags) {
     int64_t count = (int64_t)flags[ERR_MLP_FIXROWS];
-    if (count > queue_cap) count = queue_cap;
+    if (count > rows_cap) count = rows_cap;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < count; r += (int64_t)gridDim.x * blockDim.x) {
         int64_t i = fix_rows[r];
         uint32_t* row = rows + row_start[i];
@@ -777,7 +832,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         PCT_TRY(c->mlp_rec.alloc(sizeof(MlpRec) * n));
         const int64_t queue_cap = n / 8 > (1 << 20) ? n / 8 : (1 << 20);
         PCT_TRY(c->mlp_queue.alloc(sizeof(MlpDeferred) * queue_cap));
-        PCT_TRY(c->mlp_fix_rows.alloc(sizeof(int64_t) * queue_cap));
+        PCT_TRY(c->mlp_fix_rows.alloc(sizeof(int64_t) * n)); /* at most one entry per row */
         MlpRec* rec = c->mlp_rec.as<MlpRec>();
         ++c->launches;
         k_mlp_bound<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->mlp_table.as<MlpTableEntry>(), kmax,
@@ -786,16 +841,25 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (bound_total > 0 ? bound_total : 1)));
         const int exact = c->cfg.mlp_exact != 0;
         const float margin = (float)c->cfg.mlp_face_margin;
-        ++c->launches;
+        /* decreasing sample-count order of the histories */
+        const int nkeys = kmax + 2;
+        PCT_TRY(c->mlp_order.alloc(sizeof(uint32_t) * n + sizeof(unsigned) * nkeys));
+        uint32_t* order = c->mlp_order.as<uint32_t>();
+        unsigned* kcnt = reinterpret_cast<unsigned*>(order + n);
+        PCT_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(unsigned) * nkeys, c->stream));
+        c->launches += 4;
+        k_kcount<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->mlp_bound.as<int64_t>(), nkeys, kcnt);
+        k_kscan<<<1, 1024, 0, c->stream>>>(nkeys, kcnt);
+        k_kplace<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->mlp_bound.as<int64_t>(), nkeys, kcnt, order);
         k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
             c->dg, n, rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
-            c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(),
-            c->mlp_queue.as<MlpDeferred>(), queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
+            c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(), c->mlp_queue.as<MlpDeferred>(),
+            queue_cap, c->mlp_fix_rows.as<int64_t>(), flags, order);
         c->launches += 2;
         k_mlp_fix<<<4 * 152, 128, 0, c->stream>>>(c->dg, rec, c->mlp_table.as<MlpTableEntry>(),
                                                   c->mlp_queue.as<MlpDeferred>(), queue_cap, flags,
                                                   c->rows.as<uint32_t>());
-        k_mlp_dedupe<<<2 * 152, 128, 0, c->stream>>>(queue_cap, c->mlp_fix_rows.as<int64_t>(),
+        k_mlp_dedupe<<<2 * 152, 128, 0, c->stream>>>(n, c->mlp_fix_rows.as<int64_t>(),
                                                      c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                      c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels, flags);
         ++c->launches;

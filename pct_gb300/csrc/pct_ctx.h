@@ -131,7 +131,7 @@ struct pct_ctx {
 
     /* MLP rows and DROP */
     DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
-    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows;             /* MLP row generation scratch */
+    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows, mlp_order;  /* MLP row generation scratch */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
