@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--drop-form", type=int, default=0, choices=[0, 1, 2],
                     help="DROP block step: 0 scatter (default), 1 sorted, 2 tiled")
+    ap.add_argument("--voxel-order", type=int, default=0, choices=[0, 1],
+                    help="internal voxel order: 0 bricks where the grid allows (default), 1 linear")
     return ap.parse_args()
 
 
@@ -206,6 +208,7 @@ def main():
     w = phantoms.cfg2(num_histories=a.histories, seed=2 + rank)
     over = dict(w.config)
     over["drop_form"] = a.drop_form
+    over["voxel_order"] = a.voxel_order
     cfg = phantoms.make_config(over)
     iters = cfg.iterations
     data, angles = phantoms.generate(w)
@@ -332,7 +335,9 @@ def main():
                                    " block %d, lambda %.2g" % (n, R, iters, cfg.block_size, cfg.lambda_),
                        "row_entries": rows, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "inputs larger than L2 (MLP rows %.1f GB)" % (rows * 4 / 1e9),
-                       "drop_form": forms[a.drop_form],
+                       "drop_form": forms[a.drop_form], "voxel_order": ["bricks", "linear"][a.voxel_order],
+                       "mlp_fp64_samples_per_step": (c1["mlp_fp64_samples"]),
+                       "mlp_queue_capacity": max(R, 1 << 20),
                        "rows_ms_per_step": mlp_s / a.steps * 1e3, "drop_ms_per_iteration": drop_iter_s * 1e3},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * 14 * 4),
                     "d2h_bytes_per_step": int(nv * 4), "seconds_per_step": e2e_t / a.e2e_steps},

@@ -99,7 +99,12 @@ typedef struct pct_config {
                                       are recomputed in binary64 (default 2e-5) */
     int drop_form;                 /* DROP block step: PCT_DROP_SCATTER (default), _SORTED or _TILED */
     int walk_exact;                /* 1: every hull-walk step in binary64 (slow path, for checks) */
+    int voxel_order;               /* internal voxel order of the MLP rows and the DROP iterate:
+                                      PCT_ORDER_AUTO (4x2x1 bricks when COLUMNS % 4 == 0 and ROWS % 2 == 0)
+                                      or PCT_ORDER_LINEAR; every array the API returns is linear */
 } pct_config;
+
+enum { PCT_ORDER_AUTO = 0, PCT_ORDER_LINEAR = 1 };
 
 /* DROP block step forms; all compute the same block update.  SCATTER adds
  * every row entry's update with a binary32 reduction in L2.  SORTED is

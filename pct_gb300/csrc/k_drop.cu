@@ -209,6 +209,16 @@ __global__ void k_wepl_norm(int64_t n, const float* __restrict__ wepl, double* _
     }
 }
 
+/* The iterate between the linear and the brick voxel order. */
+__global__ void k_image_to_brick(DevGeom g, const float* __restrict__ lin, float* __restrict__ brk) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < g.num_voxels) brk[dev_to_brick(g, (uint32_t)v)] = lin[v];
+}
+__global__ void k_image_from_brick(DevGeom g, const float* __restrict__ brk, float* __restrict__ lin) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < g.num_voxels) lin[v] = brk[dev_to_brick(g, (uint32_t)v)];
+}
+
 }  // namespace
 
 /* Per-block voxel counts for the scatter form. */
@@ -277,13 +287,14 @@ static void enqueue_iteration(pct_ctx* c, double* resid) {
         }
         unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
         const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
+        float* xi = c->dg.brick ? c->x_brick.as<float>() : c->x.as<float>(); /* the rows' voxel order */
         k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                           c->rows.as<uint32_t>(), c->chord.as<float>(),
                                                           c->inv_norm.as<double>(), c->h.wepl.as<float>(),
-                                                          c->cfg.lambda, c->x.as<float>(), c->x_update.as<float>(),
+                                                          c->cfg.lambda, xi, c->x_update.as<float>(),
                                                           (uint32_t)nv, resid);
         k_drop_relax<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(nv, c->block_diag.as<uint32_t>() + (size_t)k * nv,
-                                                                   c->x.as<float>(), c->x_update.as<float>());
+                                                                   xi, c->x_update.as<float>());
     }
 }
 
@@ -328,6 +339,12 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
     }
     PCT_TRY(c->x_update.alloc(sizeof(float) * nv));
     PCT_CUDA(cudaMemsetAsync(c->x_update.p, 0, sizeof(float) * nv, c->stream));
+    const bool brick = c->dg.brick && c->drop_mode != PCT_DROP_TILED;
+    if (brick) {
+        PCT_TRY(c->x_brick.alloc(sizeof(float) * nv));
+        ++c->launches;
+        k_image_to_brick<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(c->dg, c->x.as<float>(), c->x_brick.as<float>());
+    }
     const int maxit = 64;
     /* [0, maxit): per-iteration squared residual, maxit: accumulator, maxit+1: ||b||^2 */
     PCT_TRY(c->drop_resid.alloc(sizeof(double) * (maxit + 2)));
@@ -356,6 +373,10 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
         }
     }
     PCT_CUDA(cudaEventRecord(e1, c->stream));
+    if (brick) {
+        ++c->launches;
+        k_image_from_brick<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(c->dg, c->x_brick.as<float>(), c->x.as<float>());
+    }
     PCT_CUDA(cudaGetLastError());
     PCT_CUDA(cudaMemcpyAsync(res_host, d_res, sizeof(double) * (maxit + 2), cudaMemcpyDeviceToHost, c->stream));
     PCT_CUDA(cudaStreamSynchronize(c->stream));

@@ -104,7 +104,7 @@ __device__ __forceinline__ int tile_voxel(const TileGeom& T, int ox, int oy, int
 
 /* Build pass 1: segments per row, and per (block, tile, row mod 32) the segment
  * and entry counts packed as (segments << 32) | entries. */
-__global__ void k_tile_count(int64_t n, int64_t B, TileGeom T, const int64_t* __restrict__ row_start,
+__global__ void k_tile_count(DevGeom dg, int64_t n, int64_t B, TileGeom T, const int64_t* __restrict__ row_start,
                              const int* __restrict__ row_len, const uint32_t* __restrict__ rows,
                              int64_t* __restrict__ row_nseg, unsigned long long* __restrict__ bt_cnt) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,7 +114,7 @@ __global__ void k_tile_count(int64_t n, int64_t B, TileGeom T, const int64_t* __
     const int len = row_len[i];
     int cur = -1, seg = 0, nseg = 0;
     for (int k = 0; k < len; ++k) {
-        uint32_t v = rows[a + k];
+        uint32_t v = dev_from_brick(dg, rows[a + k]); /* linear order */
         if (v >= (uint32_t)T.nv) continue;
         int t, l;
         tile_of(T, v, &t, &l);
@@ -139,7 +139,7 @@ __global__ void k_tile_count(int64_t n, int64_t B, TileGeom T, const int64_t* __
  * (block, tile, row mod 32) hands out the segment slot and its entry range
  * together, so the entries of consecutive segments are consecutive; the 32
  * cursors of a (block, tile) own consecutive ranges. */
-__global__ void k_tile_fill(int64_t n, int64_t B, TileGeom T, const int64_t* __restrict__ row_start,
+__global__ void k_tile_fill(DevGeom dg, int64_t n, int64_t B, TileGeom T, const int64_t* __restrict__ row_start,
                             const int* __restrict__ row_len, const uint32_t* __restrict__ rows,
                             const int64_t* __restrict__ row_seg_off, const int64_t* __restrict__ seg_sub,
                             const int64_t* __restrict__ ent_sub, const int64_t* __restrict__ ent_base,
@@ -156,7 +156,7 @@ __global__ void k_tile_fill(int64_t n, int64_t B, TileGeom T, const int64_t* __r
         int t = -1, l = 0;
         bool in = false;
         if (k < len) {
-            uint32_t v = rows[a + k];
+            uint32_t v = dev_from_brick(dg, rows[a + k]); /* linear order */
             if (v >= (uint32_t)T.nv) continue;
             tile_of(T, v, &t, &l);
             in = true;
@@ -172,7 +172,7 @@ __global__ void k_tile_fill(int64_t n, int64_t B, TileGeom T, const int64_t* __r
                 seg_ent[g] = (uint32_t)(e0 - ent_base[b]);
                 int m = 0;
                 for (int kk = k0; m < seg; ++kk) {
-                    uint32_t vv = rows[a + kk];
+                    uint32_t vv = dev_from_brick(dg, rows[a + kk]);
                     if (vv >= (uint32_t)T.nv) continue;
                     int tt, ll;
                     tile_of(T, vv, &tt, &ll);
@@ -424,7 +424,7 @@ pct_status pct_drop_tiled_build(pct_ctx* c) {
     PCT_TRY(d.bt_cnt.alloc(sizeof(unsigned long long) * nbts));
     PCT_CUDA(cudaMemsetAsync(d.bt_cnt.p, 0, sizeof(unsigned long long) * nbts, c->stream));
     ++c->launches;
-    k_tile_count<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(n, B, T, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+    k_tile_count<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, B, T, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                              c->rows.as<uint32_t>(), d.row_nseg.as<int64_t>(),
                                                              d.bt_cnt.as<unsigned long long>());
     int64_t total_slots = 0;
@@ -506,7 +506,7 @@ pct_status pct_drop_tiled_build(pct_ctx* c) {
     /* pass 2: fill */
     ++c->launches;
     k_tile_fill<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
-        n, B, T, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), d.row_seg_off.as<int64_t>(),
+        c->dg, n, B, T, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), d.row_seg_off.as<int64_t>(),
         d.seg_sub.as<int64_t>(), d.ent_sub.as<int64_t>(), d.ent_base.as<int64_t>(), d.cursor.as<unsigned long long>(),
         d.seg_row.as<uint32_t>(), d.seg_slot.as<uint32_t>(), d.seg_ent.as<uint32_t>(), d.ent.as<uint16_t>());
     /* diagonal weights */

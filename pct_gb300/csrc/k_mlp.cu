@@ -474,11 +474,9 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
                                                   uint32_t* __restrict__ rows, int* __restrict__ row_len,
                                                   MlpDeferred* __restrict__ queue, int64_t queue_cap,
                                                   int64_t* __restrict__ fix_rows,
-                                                  unsigned long long* __restrict__ flags,
-                                                  const uint32_t* __restrict__ order) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int64_t i = order ? (int64_t)order[t] : t;
+                                                  unsigned long long* __restrict__ flags) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
     const MlpRec& R = rec[i];
     const double u_2 = R.m.u_2;
     const int K = dev_sample_count(tab, kmax, u_2, g.mlp_u_step);
@@ -486,14 +484,14 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
     int64_t out = row_start[i];
     int len = 0;
     uint32_t prev = first_voxel[i];
-    rows[out + len++] = prev;
+    rows[out + len++] = dev_to_brick(g, prev);
     int fp64_samples = 0, deferred = 0, outside = prev >= nv;
     if (exact) {
         for (int k = 0; k < K; ++k) {
             uint32_t v = dev_mlp_voxel_rec(g, &R, tab[k].u1);
             ++fp64_samples;
             if (v != prev) {
-                rows[out + len++] = v;
+                rows[out + len++] = dev_to_brick(g, v);
                 prev = v;
                 outside += v >= nv;
             }
@@ -520,7 +518,7 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
             if (k + 1 < K) nxt = dev_mlp_sample(g, f, tab[k + 1], margin);
             if (cur.state == SAMPLE_CERTAIN) {
                 if (force || cur.v != prev) {
-                    rows[out + len++] = cur.v;
+                    rows[out + len++] = dev_to_brick(g, cur.v);
                     prev = cur.v;
                     outside += cur.v >= nv;
                     force = 0;
@@ -545,7 +543,7 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
                     /* queue full: binary64 here */
                     uint32_t v = dev_mlp_voxel_rec(g, &R, tab[k].u1);
                     if (force || v != prev) {
-                        rows[out + len++] = v;
+                        rows[out + len++] = dev_to_brick(g, v);
                         prev = v;
                         outside += v >= nv;
                         force = 0;
@@ -565,59 +563,6 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
     if (fp64_samples) atomicAdd(flags + ERR_MLP_FP64, (unsigned long long)fp64_samples);
 }
 
-/* Histories in decreasing order of sample count, so that the 32 rows of a
- * warp of k_mlp_fast have nearly the same length (a counting sort by the slot
- * size bound[i] = K_i + 1; the order within one count does not matter). */
-__global__ void k_kcount(int64_t n, const int64_t* __restrict__ bound, int nkeys, unsigned* __restrict__ cnt) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int64_t b = bound[i];
-    int key = b < nkeys ? (int)(nkeys - 1 - b) : 0; /* decreasing */
-    atomicAdd(cnt + key, 1u);
-}
-
-/* exclusive scan of nkeys counts in one CTA (nkeys is a few thousand) */
-__global__ void k_kscan(int nkeys, unsigned* __restrict__ cnt) {
-    __shared__ unsigned ws[32];
-    __shared__ unsigned carry_s;
-    if (threadIdx.x == 0) carry_s = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int base = 0; base < nkeys; base += blockDim.x) {
-        int k = base + threadIdx.x;
-        unsigned v = k < nkeys ? cnt[k] : 0u, x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) ws[w] = x;
-        __syncthreads();
-        if (w == 0) {
-            unsigned t = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0u;
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned y = __shfl_up_sync(0xffffffffu, t, o);
-                if (lane >= o) t += y;
-            }
-            ws[lane] = t;
-        }
-        __syncthreads();
-        unsigned incl = x + (w > 0 ? ws[w - 1] : 0u);
-        if (k < nkeys) cnt[k] = carry_s + incl - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry_s += incl;
-        __syncthreads();
-    }
-}
-
-__global__ void k_kplace(int64_t n, const int64_t* __restrict__ bound, int nkeys, unsigned* __restrict__ cursor,
-                         uint32_t* __restrict__ order) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int64_t b = bound[i];
-    int key = b < nkeys ? (int)(nkeys - 1 - b) : 0;
-    order[atomicAdd(cursor + key, 1u)] = (uint32_t)i;
-}
-
 /* The queued samples in binary64, one thread each. */
 __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __restrict__ rec,
                                                  const MlpTableEntry* __restrict__ tab,
@@ -629,7 +574,7 @@ __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __rest
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
         MlpDeferred d = queue[q];
         MlpSetup m = rec[d.hist].m;
-        rows[d.pos] = (uint32_t)dev_mlp_voxel(g, m, tab[d.k].u1);
+        rows[d.pos] = dev_to_brick(g, (uint32_t)dev_mlp_voxel(g, m, tab[d.k].u1));
     }
 }
 
@@ -656,13 +601,13 @@ __global__ void k_mlp_dedupe(int64_t rows_cap, const int64_t* __restrict__ fix_r
 }
 
 /* Dense copy of the bounded rows (for pct_get_array). */
-__global__ void k_pack_rows(int64_t n, const int64_t* __restrict__ start, const int* __restrict__ len,
+__global__ void k_pack_rows(DevGeom g, int64_t n, const int64_t* __restrict__ start, const int* __restrict__ len,
                             const int64_t* __restrict__ dense_off, const uint32_t* __restrict__ rows,
                             uint32_t* __restrict__ dense) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int64_t s = start[i], d = dense_off[i];
-    for (int j = 0; j < len[i]; ++j) dense[d + j] = rows[s + j];
+    for (int j = 0; j < len[i]; ++j) dense[d + j] = dev_from_brick(g, rows[s + j]); /* linear order */
 }
 
 __global__ void k_len64(int64_t n, const int* __restrict__ len, int64_t* __restrict__ out) {
@@ -830,7 +775,8 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
     if (n > 0) {
         PCT_TRY(c->mlp_bound.alloc(sizeof(int64_t) * n));
         PCT_TRY(c->mlp_rec.alloc(sizeof(MlpRec) * n));
-        const int64_t queue_cap = n / 8 > (1 << 20) ? n / 8 : (1 << 20);
+        /* about 0.3 samples per row need binary64 on the scan geometries; one slot per row */
+        const int64_t queue_cap = n > (1 << 20) ? n : (1 << 20);
         PCT_TRY(c->mlp_queue.alloc(sizeof(MlpDeferred) * queue_cap));
         PCT_TRY(c->mlp_fix_rows.alloc(sizeof(int64_t) * n)); /* at most one entry per row */
         MlpRec* rec = c->mlp_rec.as<MlpRec>();
@@ -841,20 +787,11 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (bound_total > 0 ? bound_total : 1)));
         const int exact = c->cfg.mlp_exact != 0;
         const float margin = (float)c->cfg.mlp_face_margin;
-        /* decreasing sample-count order of the histories */
-        const int nkeys = kmax + 2;
-        PCT_TRY(c->mlp_order.alloc(sizeof(uint32_t) * n + sizeof(unsigned) * nkeys));
-        uint32_t* order = c->mlp_order.as<uint32_t>();
-        unsigned* kcnt = reinterpret_cast<unsigned*>(order + n);
-        PCT_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(unsigned) * nkeys, c->stream));
-        c->launches += 4;
-        k_kcount<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->mlp_bound.as<int64_t>(), nkeys, kcnt);
-        k_kscan<<<1, 1024, 0, c->stream>>>(nkeys, kcnt);
-        k_kplace<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->mlp_bound.as<int64_t>(), nkeys, kcnt, order);
+        ++c->launches;
         k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
             c->dg, n, rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
             c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(), c->mlp_queue.as<MlpDeferred>(),
-            queue_cap, c->mlp_fix_rows.as<int64_t>(), flags, order);
+            queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
         c->launches += 2;
         k_mlp_fix<<<4 * 152, 128, 0, c->stream>>>(c->dg, rec, c->mlp_table.as<MlpTableEntry>(),
                                                   c->mlp_queue.as<MlpDeferred>(), queue_cap, flags,
@@ -892,7 +829,7 @@ pct_status pct_rows_dense(pct_ctx* c, int64_t* total, DevBuf* dense_off, DevBuf*
     PCT_TRY(st);
     if (dense) {
         PCT_TRY(dense->alloc(sizeof(uint32_t) * (*total > 0 ? *total : 1)));
-        k_pack_rows<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+        k_pack_rows<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                                  dense_off->as<int64_t>(), c->rows.as<uint32_t>(),
                                                                  dense->as<uint32_t>());
         PCT_CUDA(cudaGetLastError());

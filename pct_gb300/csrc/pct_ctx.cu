@@ -91,6 +91,10 @@ DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g) {
     d.t_bin_size = c.t_bin_size; d.v_bin_size = c.v_bin_size; d.angular_bin_size = c.angular_bin_size;
     d.gantry_angle_interval = c.gantry_angle_interval; d.source_radius = c.source_radius;
     d.slice_thickness = c.slice_thickness;
+    d.brick = (c.voxel_order == PCT_ORDER_AUTO && g.columns % 4 == 0 && g.rows % 2 == 0) ? 1 : 0;
+    /* exact for n < 2^31 since 64 >= 31 + log2(d) */
+    d.div_c = g.columns > 1 ? (~0ull) / (unsigned long long)g.columns + 1ull : 0ull;
+    d.div_r = g.rows > 1 ? (~0ull) / (unsigned long long)g.rows + 1ull : 0ull;
     return d;
 }
 
@@ -246,6 +250,8 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     int e = pct_geometry_derive(cfg, &g);
     if (e) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: invalid geometry (code %d)", e);
     if (cfg->block_size <= 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: block_size must be positive");
+    if (cfg->voxel_order != PCT_ORDER_AUTO && cfg->voxel_order != PCT_ORDER_LINEAR)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_create: voxel_order %d", cfg->voxel_order);
     if (cfg->drop_form < PCT_DROP_SCATTER || cfg->drop_form > PCT_DROP_TILED)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_form %d", cfg->drop_form);
     if (cfg->mlp_hull < 0 || cfg->mlp_hull > 3) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: bad mlp_hull");
@@ -287,8 +293,8 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->sc_hull, &c->msc_counts, &c->sm_counts, &c->msc_hull, &c->sm_hull, &c->fbp_image,
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
                      &c->rows, &c->chord, &c->inv_norm, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
-                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order,
-                     &c->drop_perm, &c->drop_sort};
+                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows,
+                     &c->drop_perm, &c->drop_sort, &c->x_brick};
     for (DevBuf* b : all) b->release();
     c->td.release();
     for (auto& b : c->in13) b.release();

@@ -76,6 +76,8 @@ struct DevGeom {
     double voxel_width, voxel_height, voxel_thickness;
     double x_zero, y_zero, z_zero, mlp_u_step;
     double t_bin_size, v_bin_size, angular_bin_size, gantry_angle_interval, source_radius, slice_thickness;
+    int brick; /* MLP rows and the DROP iterate use the 4x2x1 brick voxel order (see pct_device.cuh) */
+    unsigned long long div_c, div_r; /* ceil(2^64 / COLUMNS), ceil(2^64 / ROWS): q = umulhi64(n, m) */
 };
 
 enum Stage {
@@ -128,10 +130,11 @@ struct pct_ctx {
     /* voxels */
     DevBuf sc_hull, msc_counts, sm_counts, msc_hull, sm_hull;
     DevBuf fbp_image, fbp_hull, x_hull, x_hull_filtered, x0, x, x_update;
+    DevBuf x_brick;                /* the iterate in brick order while DROP runs */
 
     /* MLP rows and DROP */
     DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
-    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows, mlp_order;  /* MLP row generation scratch */
+    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows;             /* MLP row generation scratch */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */

@@ -66,6 +66,37 @@ __device__ __forceinline__ void dev_flag(unsigned long long* flags, int which) {
     atomicAdd(flags + which, 1ull);
 }
 
+/* Brick voxel order of the MLP rows and the DROP iterate: 4x2x1 voxel bricks
+ * (one 32-byte sector of floats), bricks in x, y, z order.  A path step in x
+ * or y then stays in the same sector more often than in the linear order, so
+ * the DROP gathers and reductions touch fewer L2 sectors.  Indices >= the
+ * voxel count (row entries outside the image) are kept as they are. */
+__host__ __device__ __forceinline__ uint32_t dev_brick_xyz(uint32_t C, uint32_t R, uint32_t x, uint32_t y, uint32_t z) {
+    return (((x >> 2) + (C >> 2) * ((y >> 1) + (R >> 1) * z)) << 3) | (x & 3u) | ((y & 1u) << 2);
+}
+__host__ __device__ __forceinline__ uint32_t dev_div(uint32_t n, uint32_t d, unsigned long long m) {
+#if defined(__CUDA_ARCH__)
+    return d > 1 ? (uint32_t)__umul64hi((unsigned long long)n, m) : n;
+#else
+    (void)m;
+    return n / d;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t dev_to_brick(const DevGeom& g, uint32_t v) {
+    if (!g.brick || v >= (uint32_t)g.num_voxels) return v;
+    const uint32_t C = (uint32_t)g.columns, R = (uint32_t)g.rows;
+    const uint32_t r = dev_div(v, C, g.div_c), x = v - r * C, z = dev_div(r, R, g.div_r), y = r - z * R;
+    return dev_brick_xyz(C, R, x, y, z);
+}
+__host__ __device__ __forceinline__ uint32_t dev_from_brick(const DevGeom& g, uint32_t b) {
+    if (!g.brick || b >= (uint32_t)g.num_voxels) return b;
+    const uint32_t C4 = (uint32_t)g.columns >> 2, R2 = (uint32_t)g.rows >> 1;
+    const uint32_t w = b & 7u, q = b >> 3;
+    const uint32_t t = q / C4, bx = q - t * C4, z = t / R2, by = t - z * R2;
+    const uint32_t x = bx * 4u + (w & 3u), y = by * 2u + (w >> 2);
+    return x + (uint32_t)g.columns * (y + (uint32_t)g.rows * z);
+}
+
 static inline unsigned pct_grid_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     return (unsigned)(b > 0 ? b : 1);

@@ -102,6 +102,7 @@ PCT_GFN void pct_config_fill_defaults(pct_config* c) {
     c->mlp_face_margin = 2e-5;
     c->drop_form = PCT_DROP_SCATTER;
     c->walk_exact = 0;
+    c->voxel_order = PCT_ORDER_AUTO;
 }
 
 /* Returns 0 on success, nonzero when a derived size is out of range. */
