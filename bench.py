@@ -112,6 +112,19 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def reduce_across_ranks(seconds, units, dist=None, device="cpu"):
+    """Replica aggregation: the slowest rank's time and the work of all ranks
+    (each rank runs its own scan; there is no data-path exchange)."""
+    if dist is None:
+        return float(seconds), float(units)
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def host_info():
     cpu = "unknown"
     try:
@@ -250,15 +263,12 @@ def main():
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    t = ev0.elapsed_time(ev1) * 1e-3
-    if dist:
-        tt = torch.tensor([t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t_local = ev0.elapsed_time(ev1) * 1e-3
+    t, units = reduce_across_ranks(t_local, R * iters * a.steps, dist, dev)
     c1 = r.counts()
     launches = c1["kernel_launches"] - c0["kernel_launches"]
     rows = c1["row_entries"]
-    value = R * iters * a.steps / t * ws
+    value = units / t
     mlp_s = t - drop_s
     drop_iter_s = drop_s / (a.steps * iters)
 
@@ -314,7 +324,8 @@ def main():
         q._call("pct_get_array", recon.ARRAY_ID["X"], C.c_void_p(xhost.data_ptr()), C.byref(nb))
         e2e_t += time.perf_counter() - t0
         q.close()
-    e2e_value = R * iters * a.e2e_steps / e2e_t * ws
+    e2e_t, e2e_units = reduce_across_ranks(e2e_t, R * iters * a.e2e_steps, dist, dev)
+    e2e_value = e2e_units / e2e_t
 
     # ---- CPU baseline (rank 0, bounded sample) -------------------------------------------
     cpu_b = None
