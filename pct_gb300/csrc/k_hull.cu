@@ -165,7 +165,6 @@ __global__ void __launch_bounds__(256) k_hull_walk(DevGeom g, int kind, double t
  * crossing and takes the step with step2/step3.  The voxel sequence is that
  * of the binary64 walk. */
 enum { AX_NONE = 0, AX_X = 1, AX_Y = 2, AX_Z = 3 };
-constexpr float WU = 1.2e-7f; /* twice the binary32 unit roundoff */
 
 struct WalkLine {
     double xs, ys, zs;
@@ -238,34 +237,6 @@ __device__ __forceinline__ void walk_to32(const Walk& w, Walk32& f) {
     f.xt = (float)w.x_to_go; f.yt = (float)w.y_to_go; f.zt = (float)w.z_to_go;
     f.ex = WU * fabsf(f.x); f.ey = WU * fabsf(f.y); f.ez = WU * fabsf(f.z);
     f.ext = WU * f.xt; f.eyt = WU * f.yt; f.ezt = WU * f.zt;
-}
-
-/* edge_coordinate_GPU in binary32 and a bound on its error */
-__device__ __forceinline__ float edge32(float zero, int voxel_entered, float size, int inc, int step, float* err) {
-    int on_edge = (step == inc) ? voxel_entered : voxel_entered + 1;
-    float k = (float)(inc * on_edge);
-    float prod = k * size;
-    float e = zero + prod;
-    *err = WU * (fabsf(zero) + 2.0f * fabsf(prod) + fabsf(e));
-    return e;
-}
-
-/* corresponding_coordinate in binary32: m (p - p0) + q0 with |error of p| <= ep */
-__device__ __forceinline__ float corr32(float m, float p, float p0, float q0, float ep, float* err) {
-    float d = p - p0;
-    float md = m * d;
-    float r = md + q0;
-    *err = fabsf(m) * (ep + WU * fabsf(d)) + WU * (fabsf(md) + fabsf(r));
-    return r;
-}
-
-/* a <= b decided with certainty: 1 / 0, or -1 when the bounds overlap */
-__device__ __forceinline__ int cmp_le(float a, float ea, float b, float eb) {
-    float d = b - a;
-    float tol = ea + eb + WU * (fabsf(a) + fabsf(b));
-    if (d > tol) return 1;
-    if (-d > tol) return 0;
-    return -1;
 }
 
 /* One walk step in binary32; returns false (state untouched) when a decision is uncertain. */

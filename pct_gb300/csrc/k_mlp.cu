@@ -131,6 +131,337 @@ __device__ int dev_find_endpoint(const DevGeom& g, const uint8_t* __restrict__ i
     return hit;
 }
 
+/* ---- certified binary32 endpoint walk ---------------------------------------------
+ * The walk of dev_find_endpoint, taken in binary32 with error bounds the way
+ * k_hull_walk_fast takes the hull walks: the state after a step depends only on
+ * the axis crossed and the voxel indices, so a step whose decision (or exact
+ * zero test) the bounds cannot certify is taken in binary64 from the rebuilt
+ * binary64 state.  The slopes come from binary32 sincosf/tanf of the binary32
+ * angle with a bound that covers the angle's rounding and a generous 16-ulp
+ * allowance for the functions; the binary64 slopes (pct_tan, as the reference
+ * computes them) are formed only for a binary64 step and for the hull point,
+ * which is rebuilt in binary64 from the last crossing. */
+enum { EAX_NONE = 0, EAX_X = 1, EAX_Y = 2, EAX_Z = 3 };
+constexpr float EU = 1.2e-7f; /* twice the binary32 unit roundoff */
+
+struct EpLine64 {
+    double xs, ys, zs;
+    double dy_dx, dz_dx, dz_dy, dx_dy, dx_dz, dy_dz, delta_yx;
+    int xm, ym, zm;
+};
+
+__device__ __noinline__ void ep_slopes64(double xy_angle, double xz_angle, EpLine64& L) {
+    double txy = pct_tan(xy_angle), txz = pct_tan(xz_angle);
+    L.delta_yx = fabs(txy);
+    L.dy_dx = txy;
+    L.dz_dx = txz;
+    L.dz_dy = txz / txy;
+    L.dx_dy = 1.0 / txy;
+    L.dx_dz = 1.0 / txz;
+    L.dy_dz = txy / txz;
+}
+
+/* binary64 state after crossing axis a with indices (ax, ay, az), as the
+ * loops of dev_find_endpoint compute it (zero-distance adjustments applied) */
+__device__ __noinline__ void ep_state64(const DevGeom& g, const EpLine64& L, int a, int ax, int ay, int az, double z0,
+                                        double zt0, double* x, double* y, double* z, double* xt, double* yt,
+                                        double* zt, int* vx, int* vy, int* vz) {
+    const bool is3d = L.zm != 0;
+    *vx = ax;
+    *vy = ay;
+    *vz = az;
+    if (a == EAX_NONE) {
+        *x = L.xs;
+        *y = L.ys;
+        *z = L.zs;
+        *xt = dev_distance_remaining(g.x_zero, *x, PCT_X_INC, L.xm, g.voxel_width, *vx);
+        *yt = dev_distance_remaining(g.y_zero, *y, PCT_Y_INC, L.ym, g.voxel_height, *vy);
+        *zt = dev_distance_remaining(g.z_zero, *z, PCT_Z_INC, L.zm, g.voxel_thickness, *vz);
+        return;
+    }
+    if (is3d) {
+        if (a == EAX_Z) {
+            *z = dev_edge_coordinate(g.z_zero, *vz, g.voxel_thickness, PCT_Z_INC, L.zm);
+            *x = dev_corresponding(L.dx_dz, *z, L.zs, L.xs);
+            *y = dev_corresponding(L.dy_dz, *z, L.zs, L.ys);
+            *xt = dev_distance_remaining(g.x_zero, *x, PCT_X_INC, L.xm, g.voxel_width, *vx);
+            *yt = dev_distance_remaining(g.y_zero, *y, PCT_Y_INC, L.ym, g.voxel_height, *vy);
+            *zt = g.voxel_thickness;
+        } else if (a == EAX_X) {
+            *x = dev_edge_coordinate(g.x_zero, *vx, g.voxel_width, PCT_X_INC, L.xm);
+            *y = dev_corresponding(L.dy_dx, *x, L.xs, L.ys);
+            *z = dev_corresponding(L.dz_dx, *x, L.xs, L.zs);
+            *xt = g.voxel_width;
+            *yt = dev_distance_remaining(g.y_zero, *y, PCT_Y_INC, L.ym, g.voxel_height, *vy);
+            *zt = dev_distance_remaining(g.z_zero, *z, PCT_Z_INC, L.zm, g.voxel_thickness, *vz);
+        } else {
+            *y = dev_edge_coordinate(g.y_zero, *vy, g.voxel_height, PCT_Y_INC, L.ym);
+            *x = dev_corresponding(L.dx_dy, *y, L.ys, L.xs);
+            *z = dev_corresponding(L.dz_dy, *y, L.ys, L.zs);
+            *xt = dev_distance_remaining(g.x_zero, *x, PCT_X_INC, L.xm, g.voxel_width, *vx);
+            *yt = g.voxel_height;
+            *zt = dev_distance_remaining(g.z_zero, *z, PCT_Z_INC, L.zm, g.voxel_thickness, *vz);
+        }
+        if (*xt == 0) { *xt = g.voxel_width; *vx += L.xm; }
+        if (*yt == 0) { *yt = g.voxel_height; *vy -= L.ym; }
+        if (*zt == 0) { *zt = g.voxel_thickness; *vz -= L.zm; }
+        if (*vz < 0) *vz = 0;
+    } else {
+        *z = z0;
+        *zt = zt0;
+        if (a == EAX_X) {
+            *x = dev_edge_coordinate(g.x_zero, *vx, g.voxel_width, PCT_X_INC, L.xm);
+            *y = dev_corresponding(L.dy_dx, *x, L.xs, L.ys);
+            *xt = g.voxel_width;
+            *yt = dev_distance_remaining(g.y_zero, *y, PCT_Y_INC, L.ym, g.voxel_height, *vy);
+        } else {
+            /* the 2-D loop places the y edge with the z increment direction (.cu:5137) */
+            *y = dev_edge_coordinate(g.y_zero, *vy, g.voxel_height, PCT_Z_INC, L.ym);
+            *x = dev_corresponding(L.dx_dy, *y, L.ys, L.xs);
+            *xt = dev_distance_remaining(g.x_zero, *x, PCT_X_INC, L.xm, g.voxel_width, *vx);
+            *yt = g.voxel_height;
+        }
+        if (*xt == 0) { *xt = g.voxel_width; *vx += L.xm; }
+        if (*yt == 0) { *yt = g.voxel_height; *vy -= L.ym; }
+    }
+}
+
+/* binary32 slope and its absolute error bound */
+struct Slope32 {
+    float v, e;
+};
+
+__device__ __forceinline__ Slope32 sl_quot(Slope32 a, Slope32 b) {
+    Slope32 r;
+    r.v = a.v / b.v;
+    float rel = (a.e / fabsf(a.v)) + (b.e / fabsf(b.v)) + EU;
+    r.e = fabsf(r.v) * rel * 1.01f;
+    if (!(r.e < 1e30f) || !(fabsf(r.v) < 1e30f)) r.e = 3.0e38f; /* unusable: every decision goes to binary64 */
+    return r;
+}
+
+__device__ int dev_find_endpoint_fast(const DevGeom& g, const uint8_t* __restrict__ image, float xs_f, float ys_f,
+                                      float zs_f, float xy_angle_f, float xz_angle_f, double* xo, double* yo,
+                                      double* zo, int* vxo, int* vyo, int* vzo, int entering,
+                                      unsigned long long* flags, unsigned long long* exact_steps) {
+    const int C = g.columns, R = g.rows, S = g.slices;
+    const int cap = 4 * (C + R + S) + 16;
+    double xy_angle = xy_angle_f, xz_angle = xz_angle_f;
+    if (!entering) xy_angle += PCT_PI;
+    /* binary32 trigonometry with bounds */
+    const float axy = (float)xy_angle, axz = (float)xz_angle;
+    const float dxy = (float)fabs((double)axy - xy_angle), dxz = (float)fabs((double)axz - xz_angle);
+    float sxy, cxy, sxz, cxz;
+    sincosf(axy, &sxy, &cxy);
+    sincosf(axz, &sxz, &cxz);
+    const float e_sc_xy = dxy + 16.0f * EU, e_sc_xz = dxz + 16.0f * EU;
+    EpLine64 L;
+    L.xs = xs_f;
+    L.ys = ys_f;
+    L.zs = zs_f;
+    bool have64 = false;
+    /* direction signs: binary64 only when binary32 cannot tell */
+    if (fabsf(cxy) > e_sc_xy) L.xm = cxy > 0 ? 1 : -1;
+    else { double c = pct_cos(xy_angle); L.xm = (c >= 0) - (c <= 0); }
+    if (fabsf(sxy) > e_sc_xy) L.ym = sxy > 0 ? 1 : -1;
+    else { double sv = pct_sin(xy_angle); L.ym = (sv >= 0) - (sv <= 0); }
+    if (fabsf(sxz) > e_sc_xz) L.zm = sxz > 0 ? 1 : -1;
+    else { double sv = pct_sin(xz_angle); L.zm = (sv >= 0) - (sv <= 0); }
+    if (L.xm < 0) L.zm *= -1;
+    Slope32 txy, txz;
+    txy.v = tanf(axy);
+    txy.e = (1.0f + txy.v * txy.v) * (dxy + EU) + 16.0f * EU * fabsf(txy.v);
+    txz.v = tanf(axz);
+    txz.e = (1.0f + txz.v * txz.v) * (dxz + EU) + 16.0f * EU * fabsf(txz.v);
+    if (!(fabsf(txy.v) < 1e30f) || !(txy.e < 1e30f)) txy.e = 3.0e38f;
+    if (!(fabsf(txz.v) < 1e30f) || !(txz.e < 1e30f)) txz.e = 3.0e38f;
+    const Slope32 one = {1.0f, 0.0f};
+    const Slope32 dy_dx = txy, dz_dx = txz, dz_dy = sl_quot(txz, txy), dx_dy = sl_quot(one, txy),
+                  dx_dz = sl_quot(one, txz), dy_dz = sl_quot(txy, txz);
+    /* start */
+    int vx = dev_calculate_voxel(g.x_zero, L.xs, g.voxel_width);
+    int vy = dev_calculate_voxel(g.y_zero, L.ys, g.voxel_height);
+    int vz = dev_calculate_voxel(g.z_zero, L.zs, g.voxel_thickness);
+    double x64, y64, z64, xt64, yt64, zt64;
+    ep_state64(g, L, EAX_NONE, vx, vy, vz, 0.0, 0.0, &x64, &y64, &z64, &xt64, &yt64, &zt64, &vx, &vy, &vz);
+    const double z_init = z64, zt_init = zt64;
+    float x = (float)x64, y = (float)y64, z = (float)z64, xt = (float)xt64, yt = (float)yt64, zt = (float)zt64;
+    float ex = EU * fabsf(x), ey = EU * fabsf(y), ez = EU * fabsf(z), ext = EU * xt, eyt = EU * yt, ezt = EU * zt;
+    int a_axis = EAX_NONE, ax = vx, ay = vy, az = vz;
+    const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
+    const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
+    const float xs = xs_f, ys = ys_f, zs = zs_f;
+    int voxel = vx + vy * C + vz * C * R;
+    int outside = (vx >= C) || (vy >= R) || (vz >= S) || (vx < 0) || (vy < 0) || (vz < 0);
+    int hit = outside ? 0 : (image[voxel] == 1);
+    int end = outside || hit;
+    int steps = 0;
+    const bool is3d = L.zm != 0;
+    while (!end) {
+        if (++steps > cap) {
+            dev_flag(flags, ERR_WALK_CAPPED);
+            break;
+        }
+        int axis = -1;
+        if (is3d) {
+            float x_ext = fabsf(dz_dx.v) * xt, e_xe = fabsf(dz_dx.v) * ext + dz_dx.e * xt + EU * x_ext;
+            float y_ext = fabsf(dz_dy.v) * yt, e_ye = fabsf(dz_dy.v) * eyt + dz_dy.e * yt + EU * y_ext;
+            int c1 = cmp_le(zt, ezt, x_ext, e_xe), c2 = cmp_le(zt, ezt, y_ext, e_ye);
+            if (c1 >= 0 && c2 >= 0) {
+                if (c1 && c2) axis = EAX_Z;
+                else {
+                    int c3 = cmp_le(x_ext, e_xe, y_ext, e_ye);
+                    if (c3 >= 0) axis = c3 ? EAX_X : EAX_Y;
+                }
+            }
+        } else {
+            float dyx = fabsf(txy.v);
+            float y_ext = yt / dyx;
+            float e_ye = (eyt + yt * txy.e / dyx) / dyx + EU * y_ext;
+            if (!(e_ye < 1e30f)) e_ye = 3.0e38f;
+            int c = cmp_le(xt, ext, y_ext, e_ye);
+            if (c >= 0) axis = c ? EAX_X : EAX_Y;
+        }
+        bool ok = axis >= 0;
+        int nx = vx, ny = vy, nz = vz;
+        float n_x = x, n_y = y, n_z = z, n_xt = xt, n_yt = yt, n_zt = zt;
+        float n_ex = ex, n_ey = ey, n_ez = ez, n_ext = ext, n_eyt = eyt, n_ezt = ezt;
+        if (ok) {
+            float ee, e_edge;
+            if (axis == EAX_X) {
+                nx += L.xm;
+                n_x = edge32(X0, nx, VW, PCT_X_INC, L.xm, &n_ex);
+                n_y = corr32(dy_dx.v, n_x, xs, ys, n_ex, &n_ey);
+                n_ey += dy_dx.e * fabsf(n_x - xs);
+                n_xt = VW;
+                n_ext = EU * VW;
+                float ye = edge32(Y0, ny + PCT_Y_INC * L.ym, VH, PCT_Y_INC, L.ym, &ee);
+                n_yt = fabsf(ye - n_y);
+                n_eyt = ee + n_ey + EU * n_yt;
+                if (is3d) {
+                    n_z = corr32(dz_dx.v, n_x, xs, zs, n_ex, &n_ez);
+                    n_ez += dz_dx.e * fabsf(n_x - xs);
+                    float ze = edge32(Z0, nz + PCT_Z_INC * L.zm, VT, PCT_Z_INC, L.zm, &e_edge);
+                    n_zt = fabsf(ze - n_z);
+                    n_ezt = e_edge + n_ez + EU * n_zt;
+                }
+            } else if (axis == EAX_Y) {
+                ny -= L.ym;
+                n_y = edge32(Y0, ny, VH, is3d ? PCT_Y_INC : PCT_Z_INC, L.ym, &n_ey);
+                n_x = corr32(dx_dy.v, n_y, ys, xs, n_ey, &n_ex);
+                n_ex += dx_dy.e * fabsf(n_y - ys);
+                float xe = edge32(X0, nx + PCT_X_INC * L.xm, VW, PCT_X_INC, L.xm, &e_edge);
+                n_xt = fabsf(xe - n_x);
+                n_ext = e_edge + n_ex + EU * n_xt;
+                n_yt = VH;
+                n_eyt = EU * VH;
+                if (is3d) {
+                    n_z = corr32(dz_dy.v, n_y, ys, zs, n_ey, &n_ez);
+                    n_ez += dz_dy.e * fabsf(n_y - ys);
+                    float ze = edge32(Z0, nz + PCT_Z_INC * L.zm, VT, PCT_Z_INC, L.zm, &e_edge);
+                    n_zt = fabsf(ze - n_z);
+                    n_ezt = e_edge + n_ez + EU * n_zt;
+                }
+            } else {
+                nz -= L.zm;
+                n_z = edge32(Z0, nz, VT, PCT_Z_INC, L.zm, &n_ez);
+                n_x = corr32(dx_dz.v, n_z, zs, xs, n_ez, &n_ex);
+                n_ex += dx_dz.e * fabsf(n_z - zs);
+                n_y = corr32(dy_dz.v, n_z, zs, ys, n_ez, &n_ey);
+                n_ey += dy_dz.e * fabsf(n_z - zs);
+                float xe = edge32(X0, nx + PCT_X_INC * L.xm, VW, PCT_X_INC, L.xm, &e_edge);
+                n_xt = fabsf(xe - n_x);
+                n_ext = e_edge + n_ex + EU * n_xt;
+                float ye = edge32(Y0, ny + PCT_Y_INC * L.ym, VH, PCT_Y_INC, L.ym, &e_edge);
+                n_yt = fabsf(ye - n_y);
+                n_eyt = e_edge + n_ey + EU * n_yt;
+                n_zt = VT;
+                n_ezt = EU * VT;
+            }
+            /* the exact-zero distance tests and the bounds themselves must be usable */
+            if (n_xt <= n_ext || n_yt <= n_eyt || (is3d && n_zt <= n_ezt)) ok = false;
+            if (!(n_ext < 1e-3f && n_eyt < 1e-3f && (!is3d || n_ezt < 1e-3f))) ok = false;
+        }
+        if (ok) {
+            a_axis = axis;
+            ax = nx;
+            ay = ny;
+            az = nz;
+            if (is3d && nz < 0) nz = 0;
+            vx = nx; vy = ny; vz = nz;
+            x = n_x; y = n_y; z = n_z; xt = n_xt; yt = n_yt; zt = n_zt;
+            ex = n_ex; ey = n_ey; ez = n_ez; ext = n_ext; eyt = n_eyt; ezt = n_ezt;
+        } else {
+            /* binary64 step from the binary64 state of the last crossing */
+            if (!have64) {
+                ep_slopes64(xy_angle, xz_angle, L);
+                have64 = true;
+            }
+            int bx, by, bz;
+            ep_state64(g, L, a_axis, ax, ay, az, z_init, zt_init, &x64, &y64, &z64, &xt64, &yt64, &zt64, &bx, &by, &bz);
+            int ax64;
+            if (is3d) {
+                double x_ext = fabs(L.dz_dx) * xt64, y_ext = fabs(L.dz_dy) * yt64;
+                if ((zt64 <= x_ext) && (zt64 <= y_ext)) ax64 = EAX_Z;
+                else ax64 = x_ext <= y_ext ? EAX_X : EAX_Y;
+            } else {
+                ax64 = xt64 <= yt64 / L.delta_yx ? EAX_X : EAX_Y;
+            }
+            if (ax64 == EAX_X) bx += L.xm;
+            else if (ax64 == EAX_Y) by -= L.ym;
+            else bz -= L.zm;
+            a_axis = ax64;
+            ax = bx;
+            ay = by;
+            az = bz;
+            ep_state64(g, L, a_axis, ax, ay, az, z_init, zt_init, &x64, &y64, &z64, &xt64, &yt64, &zt64, &vx, &vy, &vz);
+            x = (float)x64; y = (float)y64; z = (float)z64; xt = (float)xt64; yt = (float)yt64; zt = (float)zt64;
+            ex = EU * fabsf(x); ey = EU * fabsf(y); ez = EU * fabsf(z);
+            ext = EU * xt; eyt = EU * yt; ezt = EU * zt;
+            ++*exact_steps;
+        }
+        voxel = vx + vy * C + vz * C * R;
+        outside = (vx >= C) || (vy >= R) || (vz >= S) || (vx < 0) || (vy < 0) || (vz < 0);
+        if (!outside) hit = (image[voxel] == 1);
+        end = outside || hit;
+    }
+    if (hit) {
+        /* the hull point in binary64, rebuilt from the last crossing */
+        if (!have64) ep_slopes64(xy_angle, xz_angle, L);
+        int bx, by, bz;
+        ep_state64(g, L, a_axis, ax, ay, az, z_init, zt_init, &x64, &y64, &z64, &xt64, &yt64, &zt64, &bx, &by, &bz);
+        *xo = x64;
+        *yo = y64;
+        *zo = z64;
+    }
+    *vxo = vx;
+    *vyo = vy;
+    *vzo = vz;
+    return hit;
+}
+
+__global__ void __launch_bounds__(128) k_endpoints_fast(DevGeom g, int64_t n, const uint8_t* __restrict__ hull,
+                                                        HistView h, uint8_t* __restrict__ keep,
+                                                        unsigned long long* __restrict__ flags) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double xi = 0, yi = 0, zi = 0, xo = 0, yo = 0, zo = 0;
+    int vx = 0, vy = 0, vz = 0, vx2 = 0, vy2 = 0, vz2 = 0;
+    unsigned long long exact = 0;
+    int entered = dev_find_endpoint_fast(g, hull, h.x_entry[i], h.y_entry[i], h.z_entry[i], h.xy_entry_angle[i],
+                                         h.xz_entry_angle[i], &xi, &yi, &zi, &vx, &vy, &vz, 1, flags, &exact);
+    int exited = dev_find_endpoint_fast(g, hull, h.x_exit[i], h.y_exit[i], h.z_exit[i], h.xy_exit_angle[i],
+                                        h.xz_exit_angle[i], &xo, &yo, &zo, &vx2, &vy2, &vz2, 0, flags, &exact);
+    int both = entered && exited;
+    keep[i] = (uint8_t)both;
+    h.first_voxel[i] = both ? (uint32_t)(vx + g.columns * vy + g.rows * g.columns * vz) : 0u;
+    if (both) {
+        h.x_entry[i] = (float)xi; h.y_entry[i] = (float)yi; h.z_entry[i] = (float)zi;
+        h.x_exit[i] = (float)xo; h.y_exit[i] = (float)yo; h.z_exit[i] = (float)zo;
+    }
+    if (exact) atomicAdd(flags + ERR_WALK_FP64, exact);
+}
+
 __global__ void __launch_bounds__(128) k_endpoints(DevGeom g, int64_t n, const uint8_t* __restrict__ hull, HistView h,
                                                    uint8_t* __restrict__ keep, unsigned long long* __restrict__ flags) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -714,8 +1045,12 @@ pct_status pct_stage_endpoints(pct_ctx* c) {
     if (n > 0) {
         HistView h = c->view(c->h);
         ++c->launches;
-        k_endpoints<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, c->x_hull_filtered.as<uint8_t>(), h, keep,
-                                                                 c->err_flags.as<unsigned long long>());
+        if (c->cfg.walk_exact)
+            k_endpoints<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, c->x_hull_filtered.as<uint8_t>(), h,
+                                                                     keep, c->err_flags.as<unsigned long long>());
+        else
+            k_endpoints_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
+                c->dg, n, c->x_hull_filtered.as<uint8_t>(), h, keep, c->err_flags.as<unsigned long long>());
         PCT_CUDA(cudaGetLastError());
     }
     int64_t kept = 0;

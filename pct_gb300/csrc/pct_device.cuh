@@ -97,6 +97,37 @@ __host__ __device__ __forceinline__ uint32_t dev_from_brick(const DevGeom& g, ui
     return x + (uint32_t)g.columns * (y + (uint32_t)g.rows * z);
 }
 
+/* ---- binary32 walk arithmetic with error bounds (certified walks) ---- */
+constexpr float WU = 1.2e-7f; /* twice the binary32 unit roundoff */
+
+/* edge_coordinate_GPU in binary32 and a bound on its error */
+__device__ __forceinline__ float edge32(float zero, int voxel_entered, float size, int inc, int step, float* err) {
+    int on_edge = (step == inc) ? voxel_entered : voxel_entered + 1;
+    float k = (float)(inc * on_edge);
+    float prod = k * size;
+    float e = zero + prod;
+    *err = WU * (fabsf(zero) + 2.0f * fabsf(prod) + fabsf(e));
+    return e;
+}
+
+/* corresponding_coordinate in binary32: m (p - p0) + q0 with |error of p| <= ep */
+__device__ __forceinline__ float corr32(float m, float p, float p0, float q0, float ep, float* err) {
+    float d = p - p0;
+    float md = m * d;
+    float r = md + q0;
+    *err = fabsf(m) * (ep + WU * fabsf(d)) + WU * (fabsf(md) + fabsf(r));
+    return r;
+}
+
+/* a <= b decided with certainty: 1 / 0, or -1 when the bounds overlap */
+__device__ __forceinline__ int cmp_le(float a, float ea, float b, float eb) {
+    float d = b - a;
+    float tol = ea + eb + WU * (fabsf(a) + fabsf(b));
+    if (d > tol) return 1;
+    if (-d > tol) return 0;
+    return -1;
+}
+
 static inline unsigned pct_grid_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     return (unsigned)(b > 0 ? b : 1);

@@ -62,3 +62,23 @@ def test_mlp_rows_match_binary64_at_scale():
             assert c["mlp_fp64_samples"] < 0.01 * int(rows[0][0][-1]), c
     assert np.array_equal(rows[0][0], rows[1][0])
     assert np.array_equal(rows[0][1], rows[1][1])
+
+
+def test_endpoint_walks_match_binary64():
+    w = phantoms.cfg2(num_histories=1_000_000, seed=6)
+    cfg = phantoms.make_config(w.config)
+    data, angles = phantoms.generate(w)
+    keys = ("H_X_ENTRY", "H_Y_ENTRY", "H_Z_ENTRY", "H_X_EXIT", "H_Y_EXIT", "H_Z_EXIT", "H_FIRST_VOXEL")
+    out = {}
+    for exact in (0, 1):
+        r = recon.run_full(copy_config(cfg, walk_exact=exact), data, angles)
+        c0 = r.counts()["walk_fp64_steps"]
+        r.collect_mlp_endpoints()
+        out[exact] = {k: r.array(k) for k in keys}
+        out[exact]["n"] = r.counts()["reconstruction_histories"]
+        out[exact]["fp64_steps"] = r.counts()["walk_fp64_steps"] - c0
+        r.close()
+    assert out[0]["n"] == out[1]["n"]
+    for k in keys:
+        assert out[0][k].tobytes() == out[1][k].tobytes(), k
+    assert out[0]["fp64_steps"] < 0.1 * out[0]["n"], out[0]["fp64_steps"]
