@@ -290,6 +290,20 @@ pct_status pct_pctd_write(const char* path, const float* const data13[13], int64
                           float projection_angle, float beam_energy);
 pct_status pct_process_pctd_files(pct_ctx* ctx, const char* const* paths, int num_files);
 
+/* MLP endpoint files (write_MLP_endpoints / read_MLP_endpoints, .cu:4684-4745),
+ * MLP path files (the format of the reference's CPU reconstruction,
+ * .cu:4746, 7478-7493) and raw float32 image checkpoints (the reference writes
+ * its iterates as text, .cu:8092-8134).  Reading endpoints replaces the
+ * history store and leaves the context ready for pct_mlp_rows (an iterate of
+ * zeros unless one exists or pct_set_image provides one); reading paths
+ * replaces the rows of the current endpoints. */
+pct_status pct_write_mlp_endpoints(pct_ctx* ctx, const char* path);
+pct_status pct_read_mlp_endpoints(pct_ctx* ctx, const char* path);
+pct_status pct_write_mlp_paths(pct_ctx* ctx, const char* path);
+pct_status pct_read_mlp_paths(pct_ctx* ctx, const char* path);
+pct_status pct_write_image(pct_ctx* ctx, pct_array which, const char* path);
+pct_status pct_read_image(pct_ctx* ctx, const char* path);
+
 pct_status pct_config_default(pct_config* cfg);
 pct_status pct_geometry_from_config(const pct_config* cfg, pct_geometry* geo);
 const char* pct_last_error(void);

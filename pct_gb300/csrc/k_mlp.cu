@@ -1060,6 +1060,18 @@ pct_status pct_stage_endpoints(pct_ctx* c) {
     return PCT_OK;
 }
 
+/* chord lengths and 1/||a_i||^2 of the rows in place (used when rows are loaded from a file) */
+pct_status pct_stage_row_norms(pct_ctx* c) {
+    const int64_t n = c->h.n;
+    if (n == 0) return PCT_OK;
+    HistView h = c->view(c->h);
+    ++c->launches;
+    k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(), c->chord.as<float>(),
+                                                             c->inv_norm.as<double>());
+    PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
+
 pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* off, int64_t* total) {
     int64_t tiles = (n + SCAN_THREADS - 1) / SCAN_THREADS;
     DevBuf tmp;

@@ -69,6 +69,10 @@ def _declare(lib):
     lib.pct_stream.restype = vp
     lib.pct_stream.argtypes = [vp]
     lib.pct_process_pctd_files.argtypes = [vp, C.POINTER(C.c_char_p), ci]
+    for name in ("pct_write_mlp_endpoints", "pct_read_mlp_endpoints", "pct_write_mlp_paths", "pct_read_mlp_paths",
+                 "pct_read_image"):
+        getattr(lib, name).argtypes = [vp, C.c_char_p]
+    lib.pct_write_image.argtypes = [vp, ci, C.c_char_p]
 
 
 class Reconstruction:
@@ -118,6 +122,25 @@ class Reconstruction:
         """Reads PCTD v0 files (one per gantry angle) and uploads each as a chunk."""
         arr = (C.c_char_p * len(paths))(*[p.encode() for p in paths])
         self._call("pct_process_pctd_files", arr, len(paths))
+
+    # ---- files (write/read_MLP_endpoints, MLP path files, image checkpoints) -----
+    def write_mlp_endpoints(self, path):
+        self._call("pct_write_mlp_endpoints", str(path).encode())
+
+    def read_mlp_endpoints(self, path):
+        self._call("pct_read_mlp_endpoints", str(path).encode())
+
+    def write_mlp_paths(self, path):
+        self._call("pct_write_mlp_paths", str(path).encode())
+
+    def read_mlp_paths(self, path):
+        self._call("pct_read_mlp_paths", str(path).encode())
+
+    def write_image(self, path, name="X"):
+        self._call("pct_write_image", ARRAY_ID[name], str(path).encode())
+
+    def read_image(self, path):
+        self._call("pct_read_image", str(path).encode())
 
     def process_chunk_device(self, ptrs13, angle_ptr, n):
         """Device pointers (ints) to the 13 PCTD arrays and the angles."""
