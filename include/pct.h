@@ -102,7 +102,14 @@ typedef struct pct_config {
     int voxel_order;               /* internal voxel order of the MLP rows and the DROP iterate:
                                       PCT_ORDER_AUTO (4x2x1 bricks when COLUMNS % 4 == 0 and ROWS % 2 == 0)
                                       or PCT_ORDER_LINEAR; every array the API returns is linear */
+    /* DROP variants of the reference's CPU reconstruction (pCT_data.h:369-371, .cu:329-336) */
+    int drop_variant;              /* PCT_DROP_STANDARD, PCT_DROP_RED (DROP_blocks_red .cu:7998) or
+                                      PCT_DROP_ROBUST2 (DROP_blocks_robust2 / DROP_update_robust2 .cu:7871-7901) */
+    double eta;                    /* ETA (2.5) */
+    int psi_sign;                  /* PSI_SIGN (1) */
 } pct_config;
+
+enum { PCT_DROP_STANDARD = 0, PCT_DROP_RED = 1, PCT_DROP_ROBUST2 = 2 };
 
 enum { PCT_ORDER_AUTO = 0, PCT_ORDER_LINEAR = 1 };
 

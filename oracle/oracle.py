@@ -38,6 +38,8 @@ def load():
         _lib.ora_drop.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.c_int, C.c_double, C.c_void_p]
         _lib.ora_mlp_rows_mt.restype = C.c_int64
+        _lib.ora_drop_variant.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p]
         _lib.ora_drop_mt.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_int]
     return _lib
@@ -193,6 +195,16 @@ def drop(cfg, offsets, rows, chord, wepl, x0, iterations, block_size, lam, threa
     else:
         rc = load().ora_drop(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord), _p(w), iterations,
                              block_size, C.c_double(lam), _p(x))
+    assert rc == 0
+    return x
+
+
+def drop_variant(cfg, offsets, rows, chord, wepl, x0, iterations, block_size, lam, variant, eta, psi_sign):
+    """DROP_blocks_red (variant 1) or DROP_blocks_robust2 + DROP_update_robust2 (variant 2), binary64."""
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    w = np.ascontiguousarray(wepl, np.float32)
+    rc = load().ora_drop_variant(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord), _p(w),
+                                 iterations, block_size, C.c_double(lam), variant, C.c_double(eta), psi_sign, _p(x))
     assert rc == 0
     return x
 

@@ -1001,6 +1001,72 @@ int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uin
     return 0;
 }
 
+/* DROP variants of the reference's CPU reconstruction, binary64:
+ *   variant 1  DROP_blocks_red (.cu:7998-8021): each entry's update is
+ *              c lambda r / (||a||^2 + psi_j), psi_j = ((1 - x_j) eta) psi_sign,
+ *              relaxation DROP_update (.cu:8044-8055);
+ *   variant 2  DROP_blocks_robust2 / DROP_update_robust2 (.cu:7871-7901): the
+ *              standard update, and per voxel ||A||_j = sum of c^2 over the block's
+ *              entries; x_j += ||A||_j / (||A||_j + psi_j) * update_j / s_j with
+ *              psi_j = psi_sign (1 - x_j) eta.
+ * variant 0 is ora_drop. */
+int ora_drop_variant(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows,
+                     const double* chord, const float* wepl, int iterations, int block_size, double lambda,
+                     int variant, double eta, int psi_sign, double* x) {
+    if (variant == 0) return ora_drop(cfg, n, offsets, rows, chord, wepl, iterations, block_size, lambda, x);
+    if (variant != 1 && variant != 2) return 3;
+    pct_geometry g;
+    if (pct_geometry_derive(cfg, &g)) return 1;
+    const int nv = g.num_voxels;
+    double* upd = (double*)calloc((size_t)nv, sizeof(double));
+    double* norm_a = (double*)calloc((size_t)nv, sizeof(double));
+    uint32_t* cnt = (uint32_t*)calloc((size_t)nv, sizeof(uint32_t));
+    if (!upd || !cnt || !norm_a) { free(upd); free(cnt); free(norm_a); return 2; }
+    for (int it = 0; it < iterations; ++it) {
+        for (int64_t start = 0; start < n; start += block_size) {
+            int64_t end = start + block_size < n ? start + block_size : n;
+            for (int64_t i = start; i < end; ++i) {
+                double c = chord[i];
+                int64_t a = offsets[i], b = offsets[i + 1];
+                double dot = 0.0;
+                for (int64_t j = a; j < b; ++j)
+                    if (rows[j] < (uint32_t)nv) dot += x[rows[j]];
+                dot *= c;
+                double aa = (c * c) * (double)(b - a);
+                double residual = wepl[i] - dot;
+                for (int64_t j = a; j < b; ++j) {
+                    uint32_t v = rows[j];
+                    if (v >= (uint32_t)nv) continue;
+                    cnt[v] += 1;
+                    if (variant == 1) {
+                        double psi = ((1.0 - x[v]) * eta) * psi_sign;
+                        upd[v] += c * lambda * (residual / (aa + psi));
+                    } else {
+                        upd[v] += c * lambda * (residual / aa);
+                        norm_a[v] += c * c;
+                    }
+                }
+            }
+            for (int v = 0; v < nv; ++v)
+                if (cnt[v] > 0) {
+                    if (variant == 1) {
+                        x[v] += upd[v] / cnt[v];
+                    } else {
+                        double psi = psi_sign * (1 - x[v]) * eta;
+                        x[v] += (norm_a[v] / (norm_a[v] + psi)) * upd[v] / cnt[v];
+                    }
+                    upd[v] = 0.0;
+                    norm_a[v] = 0.0;
+                    cnt[v] = 0;
+                }
+        }
+    }
+    free(upd);
+    free(cnt);
+    free(norm_a);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Multithreaded forms (same results) used to time the reference algorithm  */
 /* on all host cores.                                                         */

@@ -89,6 +89,11 @@ double ora_effective_chord_length(const pct_config* cfg, double abs_angle_t, dou
 int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
              const float* wepl, int iterations, int block_size, double lambda, double* x);
 
+/* a16-a19 variants: 1 DROP_blocks_red, 2 DROP_blocks_robust2 + DROP_update_robust2 (0 = ora_drop). */
+int ora_drop_variant(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows,
+                     const double* chord, const float* wepl, int iterations, int block_size, double lambda,
+                     int variant, double eta, int psi_sign, double* x);
+
 /* Same results with `threads` OpenMP threads (per-history parallel rows;
  * per-block parallel DROP with atomic accumulation). */
 int64_t ora_mlp_rows_mt(const pct_config* cfg, int64_t n, const float* x_in, const float* y_in, const float* z_in,

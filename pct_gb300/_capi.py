@@ -39,7 +39,7 @@ class Config(C.Structure):
         ("x_k0", C.c_int), ("iterations", C.c_int), ("block_size", C.c_int), ("lambda_", C.c_float),
         ("residual_tol", C.c_double), ("chord_bf16", C.c_int), ("mlp_exact", C.c_int),
         ("mlp_face_margin", C.c_double), ("drop_form", C.c_int), ("walk_exact", C.c_int),
-        ("voxel_order", C.c_int),
+        ("voxel_order", C.c_int), ("drop_variant", C.c_int), ("eta", C.c_double), ("psi_sign", C.c_int),
     ]
 
 

@@ -44,6 +44,11 @@ __global__ void k_block_counts(int64_t start, int64_t end, const int64_t* __rest
     }
 }
 
+/* VARIANT 0: block_update_GPU; 1: DROP_blocks_red (.cu:7998-8021), the entry's
+ * update c lambda r / (||a||^2 + psi_j) with psi_j = ((1 - x_j) eta) psi_sign,
+ * in binary32; 2: DROP_blocks_robust2 (.cu:7871-7885), the standard update (its
+ * per-voxel sums of c^2 are fixed by the rows and counted once, k_block_norms). */
+template <int VARIANT>
 __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64_t end,
                                                             const uint32_t* __restrict__ perm,
                                                             const int64_t* __restrict__ row_start,
@@ -53,7 +58,8 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
                                                             const double* __restrict__ inv_norm,
                                                             const float* __restrict__ wepl, float lambda,
                                                             const float* __restrict__ x, float* __restrict__ upd,
-                                                            uint32_t nv, double* __restrict__ resid) {
+                                                            uint32_t nv, double* __restrict__ resid, float eta,
+                                                            float psi_sign) {
     __shared__ double sres[DROP_WARPS];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t i = start + (int64_t)blockIdx.x * DROP_WARPS + w;
@@ -69,10 +75,19 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
         for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
         double c = chord[i];
         double res = (double)wepl[i] - c * (double)dot;
-        float value = (float)(c * res * inv_norm[i] * (double)lambda);
-        for (int64_t p = a + lane; p < b; p += 32) {
-            uint32_t v = rows[p];
-            if (v < nv) atomicAdd(upd + v, value);
+        if (VARIANT == 1) {
+            const float cl_res = (float)(c * (double)lambda * res);
+            const float aa = (float)((c * c) * (double)(b - a));
+            for (int64_t p = a + lane; p < b; p += 32) {
+                uint32_t v = rows[p];
+                if (v < nv) atomicAdd(upd + v, cl_res / (aa + ((1.0f - x[v]) * eta) * psi_sign));
+            }
+        } else {
+            float value = (float)(c * res * inv_norm[i] * (double)lambda);
+            for (int64_t p = a + lane; p < b; p += 32) {
+                uint32_t v = rows[p];
+                if (v < nv) atomicAdd(upd + v, value);
+            }
         }
         r2 = res * res;
     }
@@ -109,6 +124,37 @@ __global__ void k_drop_relax4(int nv4, const uint4* __restrict__ cnt, float4* __
     if (s.w > 0) xv.w += u.w / (float)s.w;
     x[q] = xv;
     upd[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f); /* entries with s = 0 are already 0 */
+}
+
+/* ||A||_j of one block: the sum of c^2 over the block's entries in voxel j
+ * (DROP_blocks_robust2, .cu:7884), one warp per row. */
+__global__ void k_block_norms(int64_t start, int64_t end, const int64_t* __restrict__ row_start,
+                              const int* __restrict__ row_len, const uint32_t* __restrict__ rows,
+                              const float* __restrict__ chord, uint32_t nv, float* __restrict__ norm) {
+    int lane = threadIdx.x & 31;
+    int64_t i = start + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    if (i >= end) return;
+    const float c2 = (float)((double)chord[i] * (double)chord[i]);
+    int64_t a = row_start[i], b = a + row_len[i];
+    for (int64_t p = a + lane; p < b; p += 32) {
+        uint32_t v = rows[p];
+        if (v < nv) atomicAdd(norm + v, c2);
+    }
+}
+
+/* DROP_update_robust2 (.cu:7887-7901): x += ||A|| / (||A|| + psi) * x_update / s,
+ * psi = psi_sign (1 - x) eta. */
+__global__ void k_drop_relax_robust2(int nv, const uint32_t* __restrict__ cnt, const float* __restrict__ norm,
+                                     float* __restrict__ x, float* __restrict__ upd, float eta, float psi_sign) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    uint32_t s = cnt[v];
+    if (s > 0) {
+        float xv = x[v], na = norm[v];
+        float psi = psi_sign * (1.0f - xv) * eta;
+        x[v] = xv + (na / (na + psi)) * upd[v] / (float)s;
+        upd[v] = 0.0f;
+    }
 }
 
 /* ---- aggregated form ----------------------------------------------------------- */
@@ -252,6 +298,17 @@ static pct_status build_scatter(pct_ctx* c) {
             s, e, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), (uint32_t)nv,
             c->block_diag.as<uint32_t>() + (size_t)k * nv);
     }
+    if (c->cfg.drop_variant == PCT_DROP_ROBUST2) {
+        PCT_TRY(c->block_norm.alloc(sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1)));
+        PCT_CUDA(cudaMemsetAsync(c->block_norm.p, 0, sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
+        for (int k = 0; k < nb; ++k) {
+            int64_t s = k * B, e = s + B < n ? s + B : n;
+            ++c->launches;
+            k_block_norms<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
+                s, e, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), c->chord.as<float>(),
+                (uint32_t)nv, c->block_norm.as<float>() + (size_t)k * nv);
+        }
+    }
     PCT_CUDA(cudaGetLastError());
     c->num_blocks = nb;
     c->drop_mode = PCT_DROP_SCATTER;
@@ -304,12 +361,19 @@ static void enqueue_iteration(pct_ctx* c, double* resid) {
         unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
         const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
         float* xi = c->dg.brick ? c->x_brick.as<float>() : c->x.as<float>(); /* the rows' voxel order */
-        k_drop_rows<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+        const int var = c->cfg.drop_variant;
+        const float eta = (float)c->cfg.eta, sgn = (float)c->cfg.psi_sign;
+        auto rows_kernel = var == PCT_DROP_RED ? k_drop_rows<1> : (var == PCT_DROP_ROBUST2 ? k_drop_rows<2> : k_drop_rows<0>);
+        rows_kernel<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                           c->rows.as<uint32_t>(), c->chord.as<float>(),
                                                           c->inv_norm.as<double>(), c->h.wepl.as<float>(),
                                                           c->cfg.lambda, xi, c->x_update.as<float>(),
-                                                          (uint32_t)nv, resid);
-        if (nv % 4 == 0)
+                                                          (uint32_t)nv, resid, eta, sgn);
+        if (var == PCT_DROP_ROBUST2)
+            k_drop_relax_robust2<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(
+                nv, c->block_diag.as<uint32_t>() + (size_t)k * nv, c->block_norm.as<float>() + (size_t)k * nv, xi,
+                c->x_update.as<float>(), eta, sgn);
+        else if (nv % 4 == 0)
             k_drop_relax4<<<pct_grid_for(nv / 4, 256), 256, 0, c->stream>>>(
                 nv / 4, reinterpret_cast<const uint4*>(c->block_diag.as<uint32_t>() + (size_t)k * nv),
                 reinterpret_cast<float4*>(xi), reinterpret_cast<float4*>(c->x_update.as<float>()));

@@ -250,6 +250,10 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     int e = pct_geometry_derive(cfg, &g);
     if (e) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: invalid geometry (code %d)", e);
     if (cfg->block_size <= 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: block_size must be positive");
+    if (cfg->drop_variant < PCT_DROP_STANDARD || cfg->drop_variant > PCT_DROP_ROBUST2)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_variant %d", cfg->drop_variant);
+    if (cfg->drop_variant != PCT_DROP_STANDARD && cfg->drop_form == PCT_DROP_TILED)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_create: the DROP variants run in the scatter or sorted form");
     if (cfg->voxel_order != PCT_ORDER_AUTO && cfg->voxel_order != PCT_ORDER_LINEAR)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: voxel_order %d", cfg->voxel_order);
     if (cfg->drop_form < PCT_DROP_SCATTER || cfg->drop_form > PCT_DROP_TILED)
@@ -294,7 +298,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
                      &c->rows, &c->chord, &c->inv_norm, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
                      &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows,
-                     &c->drop_perm, &c->drop_sort, &c->x_brick};
+                     &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm};
     for (DevBuf* b : all) b->release();
     c->td.release();
     for (auto& b : c->in13) b.release();

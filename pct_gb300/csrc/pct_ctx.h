@@ -136,6 +136,7 @@ struct pct_ctx {
     DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
     DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows;             /* MLP row generation scratch */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
+    DevBuf block_norm;             /* per DROP block: sum of c^2 per voxel (robust variant) */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
     int64_t dense_total = 0;

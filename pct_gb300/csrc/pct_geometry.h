@@ -103,6 +103,9 @@ PCT_GFN void pct_config_fill_defaults(pct_config* c) {
     c->drop_form = PCT_DROP_SCATTER;
     c->walk_exact = 0;
     c->voxel_order = PCT_ORDER_AUTO;
+    c->drop_variant = PCT_DROP_STANDARD;
+    c->eta = 2.5;
+    c->psi_sign = 1;
 }
 
 /* Returns 0 on success, nonzero when a derived size is out of range. */
