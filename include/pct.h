@@ -93,7 +93,8 @@ typedef struct pct_config {
     /* GB300 extensions (no reference counterpart) */
     double residual_tol;           /* stop DROP early when the FP64 relative data
                                       residual falls below this (0: run all iterations) */
-    int chord_bf16;                /* store per-row chord lengths in bf16 (0: fp32) */
+    int chord_bf16;                /* 1: round each row's chord length to bfloat16 (nearest even) before
+                                      it enters the row norm and the DROP updates (0: binary32) */
     int mlp_exact;                 /* 1: every MLP sample in binary64 (slow path, for checks) */
     double mlp_face_margin;        /* [cm] binary32 MLP samples closer than this to a voxel face
                                       are recomputed in binary64 (default 2e-5) */

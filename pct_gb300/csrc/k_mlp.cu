@@ -17,6 +17,7 @@
  *   k_row_norms   EffectiveChordLength_GPU (.cu:4974-4995) per row and the DROP
  *                 row norm ||a_i||^2 = c^2 n (.cu:5825) kept as 1/||a_i||^2 in binary64.
  */
+#include <cuda_bf16.h>
 #include "pct_device.cuh"
 
 namespace {
@@ -962,12 +963,15 @@ __device__ double dev_chord(const DevGeom& g, double abs_angle_t, double abs_ang
     return VW * c2d * c3d;
 }
 
+/* bf16: the chord length rounded to bfloat16 (round to nearest even), the value
+ * a bf16 store holds; it then enters the row norm and the DROP updates. */
 __global__ void k_row_norms(DevGeom g, int64_t n, HistView h, const int* __restrict__ len, float* __restrict__ chord,
-                            double* __restrict__ inv_norm) {
+                            double* __restrict__ inv_norm, int bf16) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double ae = h.xy_entry_angle[i], ax = h.xy_exit_angle[i], ze = h.xz_entry_angle[i], zx = h.xz_exit_angle[i];
     double c = dev_chord(g, (ae + ax) / 2.0, (ze + zx) / 2.0);
+    if (bf16) c = (double)__bfloat162float(__float2bfloat16_rn((float)c));
     chord[i] = (float)c;
     double nn = (double)len[i];
     inv_norm[i] = 1.0 / ((c * c) * nn);
@@ -1067,7 +1071,7 @@ pct_status pct_stage_row_norms(pct_ctx* c) {
     HistView h = c->view(c->h);
     ++c->launches;
     k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(), c->chord.as<float>(),
-                                                             c->inv_norm.as<double>());
+                                                             c->inv_norm.as<double>(), c->cfg.chord_bf16);
     PCT_CUDA(cudaGetLastError());
     return PCT_OK;
 }
@@ -1148,7 +1152,8 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
                                                      c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels, flags);
         ++c->launches;
         k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(),
-                                                                 c->chord.as<float>(), c->inv_norm.as<double>());
+                                                                 c->chord.as<float>(), c->inv_norm.as<double>(),
+                                                                 c->cfg.chord_bf16);
         PCT_CUDA(cudaGetLastError());
     }
     c->row_capacity = bound_total;

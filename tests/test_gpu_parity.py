@@ -261,3 +261,41 @@ def test_drop_variants_within_tolerance(run, variant):
     err = np.linalg.norm(x - ref) / np.linalg.norm(ref)
     assert err <= DROP_TOL, "relative L2 %.3e" % err
     assert np.linalg.norm(ref - std) > 2 * DROP_TOL * np.linalg.norm(std)  # the variant changes the image
+
+
+def test_bf16_chords_error_stated(run):
+    """chord_bf16: the chord lengths are the oracle's rounded to bfloat16 bit for
+    bit; the DROP iterate is within the DROP tolerance of the binary64 run on
+    those chords, and its distance to the binary64 run on binary64 chords is
+    the stated cost of bf16 chords (printed, bounded by 2^-8 relative)."""
+    name, cfg, ora, out = run
+    its = cfg.iterations
+    if its == 0:
+        pytest.skip("no iterations")
+    cfg2 = phantoms.make_config({})
+    for f, _ in cfg._fields_:
+        setattr(cfg2, f, getattr(cfg, f))
+    cfg2.chord_bf16 = 1
+    w, _ = CASES[name]()
+    data, angles = phantoms.generate(w)
+    r = recon.run_full(cfg2, data, angles)
+    r.collect_mlp_endpoints()
+    r.mlp_rows()
+    chord = r.array("CHORD")
+    r.drop(its)
+    x = r.array("X").astype(np.float64)
+    r.close()
+    offs, rows, chord64 = oracle.mlp_rows(cfg, ora["_hr"])
+    c32 = chord64.astype(np.float32)
+    u = c32.view(np.uint32).astype(np.uint64)
+    bf = (((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16).astype(np.uint32).view(np.float32)  # round to nearest even
+    assert chord.tobytes() == bf.tobytes()
+    ref_bf = oracle.drop(cfg, offs, rows, bf.astype(np.float64), ora["_hr"]["WEPL"], ora["x_k0"], its, cfg.block_size,
+                         float(np.float32(cfg.lambda_)))
+    err_bf = np.linalg.norm(x - ref_bf) / np.linalg.norm(ref_bf)
+    ref = ora["x_%d" % its]
+    err = np.linalg.norm(x - ref) / np.linalg.norm(ref)
+    print("%s: bf16 chords, relative L2 vs binary64 on bf16 chords %.2e, vs binary64 on binary64 chords %.2e"
+          % (name, err_bf, err))
+    assert err_bf <= DROP_TOL
+    assert err <= 2.0 ** -8
