@@ -27,6 +27,7 @@ namespace {
 
 constexpr int DROP_THREADS = 256;
 constexpr int DROP_WARPS = DROP_THREADS / 32;
+constexpr int DROP_REG = 8; /* row entries per lane held in registers (256 per row) */
 
 /* ---- scatter form ------------------------------------------------------------ */
 
@@ -55,48 +56,69 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
                                                             const int* __restrict__ row_len,
                                                             const uint32_t* __restrict__ rows,
                                                             const float* __restrict__ chord,
-                                                            const double* __restrict__ inv_norm,
+                                                            const float* __restrict__ row_scale,
                                                             const float* __restrict__ wepl, float lambda,
                                                             const float* __restrict__ x, float* __restrict__ upd,
                                                             uint32_t nv, double* __restrict__ resid, float eta,
                                                             float psi_sign) {
-    __shared__ double sres[DROP_WARPS];
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t i = start + (int64_t)blockIdx.x * DROP_WARPS + w;
-    double r2 = 0.0;
-    if (i < end) {
-        if (perm) i = start + perm[i];
-        int64_t a = row_start[i], b = a + row_len[i];
+    __shared__ float sres[DROP_WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t stride = (int64_t)gridDim.x * DROP_WARPS;
+    float r2 = 0.0f; /* lane 0: this warp's rows */
+    /* persistent warps: one row at a time, its first 32 * DROP_REG entries held in
+     * registers between the dot and the update (independent loads, one read of the row) */
+    for (int64_t j = start + (int64_t)blockIdx.x * DROP_WARPS + w; j < end; j += stride) {
+        const int64_t i = perm ? start + perm[j] : j;
+        const int64_t a = row_start[i];
+        const int len = row_len[i];
+        uint32_t e[DROP_REG];
+        float xv[DROP_REG];
+#pragma unroll
+        for (int k = 0; k < DROP_REG; ++k) {
+            const int q = lane + 32 * k;
+            e[k] = q < len ? rows[a + q] : 0xffffffffu;
+        }
+#pragma unroll
+        for (int k = 0; k < DROP_REG; ++k) xv[k] = e[k] < nv ? x[e[k]] : 0.0f;
         float dot = 0.0f;
-        for (int64_t p = a + lane; p < b; p += 32) {
-            uint32_t v = rows[p];
+#pragma unroll
+        for (int k = 0; k < DROP_REG; ++k) dot += xv[k];
+        for (int q = 32 * DROP_REG + lane; q < len; q += 32) {
+            const uint32_t v = rows[a + q];
             if (v < nv) dot += x[v];
         }
         for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-        double c = chord[i];
-        double res = (double)wepl[i] - c * (double)dot;
+        /* binary32 throughout: an FP64 warp instruction costs 16 SM cycles on this part */
+        const float c = chord[i];
+        const float res = fmaf(-c, dot, wepl[i]); /* one rounding */
         if (VARIANT == 1) {
-            const float cl_res = (float)(c * (double)lambda * res);
-            const float aa = (float)((c * c) * (double)(b - a));
-            for (int64_t p = a + lane; p < b; p += 32) {
-                uint32_t v = rows[p];
+            const float cl_res = (c * lambda) * res;
+            const float aa = (c * c) * (float)len;
+#pragma unroll
+            for (int k = 0; k < DROP_REG; ++k)
+                if (e[k] < nv) atomicAdd(upd + e[k], cl_res / (aa + ((1.0f - xv[k]) * eta) * psi_sign));
+            for (int q = 32 * DROP_REG + lane; q < len; q += 32) {
+                const uint32_t v = rows[a + q];
                 if (v < nv) atomicAdd(upd + v, cl_res / (aa + ((1.0f - x[v]) * eta) * psi_sign));
             }
         } else {
-            float value = (float)(c * res * inv_norm[i] * (double)lambda);
-            for (int64_t p = a + lane; p < b; p += 32) {
-                uint32_t v = rows[p];
+            const float value = (res * row_scale[i]) * lambda;
+#pragma unroll
+            for (int k = 0; k < DROP_REG; ++k)
+                if (e[k] < nv) atomicAdd(upd + e[k], value);
+            for (int q = 32 * DROP_REG + lane; q < len; q += 32) {
+                const uint32_t v = rows[a + q];
                 if (v < nv) atomicAdd(upd + v, value);
             }
         }
-        r2 = res * res;
+        r2 += res * res;
     }
     if (lane == 0) sres[w] = r2;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.0;
+        float s = 0.0f;
         for (int k = 0; k < DROP_WARPS; ++k) s += sres[k];
-        if (s != 0.0) atomicAdd(resid, s);
+        if (s != 0.0f) atomicAdd(resid, (double)s); /* the iteration's sum in binary64 */
     }
 }
 
@@ -347,6 +369,18 @@ static pct_status build_sorted(pct_ctx* c) {
     return PCT_OK;
 }
 
+/* CTAs of a persistent k_drop_rows launch: every resident slot of the device,
+ * or fewer when the block has fewer rows than warps. */
+static unsigned drop_rows_grid(pct_ctx* c, int64_t rows, const void* fn) {
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms < 1) sms = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, DROP_THREADS, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int64_t need = (rows + DROP_WARPS - 1) / DROP_WARPS;
+    const int64_t cap = (int64_t)sms * per_sm;
+    return (unsigned)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
 /* Enqueues one DROP iteration (all blocks) on the context stream. */
 static void enqueue_iteration(pct_ctx* c, double* resid) {
     const int64_t n = c->h.n;
@@ -358,15 +392,15 @@ static void enqueue_iteration(pct_ctx* c, double* resid) {
             pct_drop_tiled_enqueue(c, k, resid);
             continue;
         }
-        unsigned grid = (unsigned)((e - s + DROP_WARPS - 1) / DROP_WARPS);
         const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
         float* xi = c->dg.brick ? c->x_brick.as<float>() : c->x.as<float>(); /* the rows' voxel order */
         const int var = c->cfg.drop_variant;
         const float eta = (float)c->cfg.eta, sgn = (float)c->cfg.psi_sign;
         auto rows_kernel = var == PCT_DROP_RED ? k_drop_rows<1> : (var == PCT_DROP_ROBUST2 ? k_drop_rows<2> : k_drop_rows<0>);
+        const unsigned grid = drop_rows_grid(c, e - s, (const void*)rows_kernel);
         rows_kernel<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                           c->rows.as<uint32_t>(), c->chord.as<float>(),
-                                                          c->inv_norm.as<double>(), c->h.wepl.as<float>(),
+                                                          c->row_scale.as<float>(), c->h.wepl.as<float>(),
                                                           c->cfg.lambda, xi, c->x_update.as<float>(),
                                                           (uint32_t)nv, resid, eta, sgn);
         if (var == PCT_DROP_ROBUST2)

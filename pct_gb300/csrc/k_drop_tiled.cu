@@ -246,23 +246,23 @@ __global__ void __launch_bounds__(FWD_THREADS) k_tile_fwd(TileGeom T, int b, int
 __global__ void __launch_bounds__(ROWS_THREADS) k_tile_rows(int64_t start, int64_t end, const int64_t* __restrict__ row_seg_off,
                                                             const long long* __restrict__ partial,
                                                             const float* __restrict__ chord,
-                                                            const double* __restrict__ inv_norm,
+                                                            const float* __restrict__ row_scale,
                                                             const float* __restrict__ wepl, float lambda,
                                                             float* __restrict__ u, unsigned* __restrict__ umax,
                                                             double* __restrict__ resid) {
-    __shared__ double sres[ROWS_THREADS / 32];
+    __shared__ float sres[ROWS_THREADS / 32];
     __shared__ unsigned smax[ROWS_THREADS / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t i = start + (int64_t)blockIdx.x * ROWS_THREADS + threadIdx.x;
-    double r2 = 0.0;
+    float r2 = 0.0f;
     unsigned mx = 0;
     if (i < end) {
         long long sum = 0;
         for (int64_t p = row_seg_off[i]; p < row_seg_off[i + 1]; ++p) sum += partial[p];
-        const double dot = (double)sum * (1.0 / 4294967296.0);
-        double c = chord[i];
-        double res = (double)wepl[i] - c * dot;
-        float val = (float)(c * res * inv_norm[i] * (double)lambda);
+        const float dot = __ll2float_rn(sum) * (1.0f / 4294967296.0f); /* exact sum, rounded once */
+        const float c = chord[i];
+        const float res = fmaf(-c, dot, wepl[i]);
+        const float val = (res * row_scale[i]) * lambda;
         u[i - start] = val;
         r2 = res * res;
         mx = __float_as_uint(fabsf(val)); /* non-negative floats order like their bits; NaN sorts above inf */
@@ -278,13 +278,13 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_tile_rows(int64_t start, int64
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.0;
+        float s = 0.0f;
         unsigned m = 0;
         for (int k = 0; k < ROWS_THREADS / 32; ++k) {
             s += sres[k];
             m = smax[k] > m ? smax[k] : m;
         }
-        if (s != 0.0) atomicAdd(resid, s);
+        if (s != 0.0f) atomicAdd(resid, (double)s);
         if (m) atomicMax(umax, m);
     }
 }
@@ -539,7 +539,7 @@ void pct_drop_tiled_enqueue(pct_ctx* c, int b, double* resid) {
             d.partial.as<long long>(), c->err_flags.as<unsigned long long>());
     cudaMemsetAsync(d.umax.as<unsigned>() + b, 0, sizeof(unsigned), c->stream);
     k_tile_rows<<<pct_grid_for(e - s, ROWS_THREADS), ROWS_THREADS, 0, c->stream>>>(
-        s, e, d.row_seg_off.as<int64_t>(), d.partial.as<long long>(), c->chord.as<float>(), c->inv_norm.as<double>(),
+        s, e, d.row_seg_off.as<int64_t>(), d.partial.as<long long>(), c->chord.as<float>(), c->row_scale.as<float>(),
         c->h.wepl.as<float>(), c->cfg.lambda, d.u.as<float>(), d.umax.as<unsigned>() + b, resid);
     k_tile_bwd<false><<<T.nt * BWD_CLUSTER, BWD_THREADS, 0, c->stream>>>(
         T, b, d.seg_bt.as<int64_t>(), d.seg_base.as<int64_t>(), d.ent_base.as<int64_t>(), d.seg_row.as<uint32_t>(),

@@ -219,7 +219,7 @@ extern "C" pct_status pct_read_mlp_paths(pct_ctx* c, const char* path) {
     PCT_TRY(c->row_len.alloc(sizeof(int) * (n > 0 ? n : 1)));
     PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (total > 0 ? total : 1)));
     PCT_TRY(c->chord.alloc(sizeof(float) * (n > 0 ? n : 1)));
-    PCT_TRY(c->inv_norm.alloc(sizeof(double) * (n > 0 ? n : 1)));
+    PCT_TRY(c->row_scale.alloc(sizeof(float) * (n > 0 ? n : 1)));
     PCT_CUDA(cudaMemcpyAsync(c->row_offsets.p, off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, c->stream));
     if (total > 0) {
         DevBuf tmp;

@@ -168,6 +168,7 @@ enum { AX_NONE = 0, AX_X = 1, AX_Y = 2, AX_Z = 3 };
 
 struct WalkLine {
     double xs, ys, zs;
+    float fxs, fys, fzs; /* the same start point (binary32 inputs) */
     double dy_dx, dz_dx, dz_dy, dx_dy, dx_dz, dy_dz;
     int xm, ym, zm;
 };
@@ -242,9 +243,9 @@ __device__ __forceinline__ void walk_to32(const Walk& w, Walk32& f) {
 /* One walk step in binary32; returns false (state untouched) when a decision is uncertain. */
 __device__ __forceinline__ bool step32(const DevGeom& g, const WalkLine& L, const float* m32, Walk32& f, int& vx,
                                        int& vy, int& vz, int& a_axis, int& ax, int& ay, int& az) {
-    const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
-    const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
-    const float xs = (float)L.xs, ys = (float)L.ys, zs = (float)L.zs;
+    const float X0 = g.fx0, Y0 = g.fy0, Z0 = g.fz0;
+    const float VW = g.fvw, VH = g.fvh, VT = g.fvt;
+    const float xs = L.fxs, ys = L.fys, zs = L.fzs;
     /* m32: dy_dx, dz_dx, dz_dy, dx_dy, dx_dz, dy_dz */
     int axis;
     if (L.zm != 0) {
@@ -345,6 +346,7 @@ __global__ void __launch_bounds__(256) k_hull_walk_fast(DevGeom g, int kind, dou
     L.ym = (ye <= yx) - (ye >= yx);
     L.zm = (ze <= zx) - (ze >= zx);
     L.xs = xe; L.ys = ye; L.zs = ze;
+    L.fxs = xe; L.fys = ye; L.fzs = ze;
     float m32[6];
     m32[0] = (yx - ye) / (xx - xe);
     m32[1] = (zx - ze) / (xx - xe);

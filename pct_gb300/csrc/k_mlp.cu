@@ -289,8 +289,8 @@ __device__ int dev_find_endpoint_fast(const DevGeom& g, const uint8_t* __restric
     float x = (float)x64, y = (float)y64, z = (float)z64, xt = (float)xt64, yt = (float)yt64, zt = (float)zt64;
     float ex = EU * fabsf(x), ey = EU * fabsf(y), ez = EU * fabsf(z), ext = EU * xt, eyt = EU * yt, ezt = EU * zt;
     int a_axis = EAX_NONE, ax = vx, ay = vy, az = vz;
-    const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
-    const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
+    const float X0 = g.fx0, Y0 = g.fy0, Z0 = g.fz0;
+    const float VW = g.fvw, VH = g.fvh, VT = g.fvt;
     const float xs = xs_f, ys = ys_f, zs = zs_f;
     int voxel = vx + vy * C + vz * C * R;
     int outside = (vx >= C) || (vy >= R) || (vz >= S) || (vx < 0) || (vy < 0) || (vz < 0);
@@ -727,9 +727,9 @@ struct MlpFast {
 
 __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpFast& f, const MlpTableEntry te,
                                                    float margin) {
-    const float X0 = (float)g.x_zero, Y0 = (float)g.y_zero, Z0 = (float)g.z_zero;
-    const float VW = (float)g.voxel_width, VH = (float)g.voxel_height, VT = (float)g.voxel_thickness;
-    const float iVW = 1.0f / VW, iVH = 1.0f / VH, iVT = 1.0f / VT;
+    const float X0 = g.fx0, Y0 = g.fy0, Z0 = g.fz0;
+    const float VW = g.fvw, VH = g.fvh, VT = g.fvt;
+    const float iVW = g.fivw, iVH = g.fivh, iVT = g.fivt;
     const float lnX0 = __logf(36.08f);
     const float* b = f.b;
     float d = (f.u2_hi - te.u1_hi) + (f.u2_lo - te.u1_lo);
@@ -749,8 +749,9 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     E1 = fmaf(E1, d, b[1] * (1.0f / 6));  E2 = fmaf(E2, d, b[1] * (2.0f / 24));  E3 = fmaf(E3, d, b[1] * (1.0f / 12));
     E1 = fmaf(E1, d, b[0] * (1.0f / 2));  E2 = fmaf(E2, d, b[0] * (2.0f / 6));   E3 = fmaf(E3, d, b[0] * (1.0f / 6));
     float D = fmaf(Q3, Q1, -Q2 * Q2);
-    float inv = 1.0f / (c2 * D);
-    float id = 1.0f / d;
+    /* approximate reciprocals (2 ulp): far inside the face margin that certifies each voxel */
+    float inv = __fdividef(1.0f, c2 * D);
+    float id = __fdividef(1.0f, d);
     float id2 = id * id, id3 = id2 * id;
     float Aa = Q1 * inv * id3;      /* (Sigma_2^-1)_00 */
     float Bm = E1 * inv * id2;      /* (R1^T Sigma_2^-1 R1)_01 */
@@ -758,7 +759,7 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     float bb = -Q2 * inv * id2;     /* (Sigma_2^-1)_01 */
     float e3 = -E3 * inv * id;      /* d (Sigma_2^-1)_01 + (Sigma_2^-1)_11 */
     float ft0 = te.s1i0 + Aa, ft1 = te.s1i1 + Bm, ft3 = te.s1i3 + Cm;
-    float idet = 1.0f / fmaf(ft0, ft3, -ft1 * ft1);
+    float idet = __fdividef(1.0f, fmaf(ft0, ft3, -ft1 * ft1));
     float beta = fmaf(ft3, Aa, -ft1 * Bm) * idet;
     float gam = fmaf(ft3, bb, -ft1 * e3) * idet;
     float ct = fmaf(beta, f.dT, gam * f.T21);
@@ -791,6 +792,59 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     return s;
 }
 
+/* Launch order for k_mlp_fast: each chunk of MLP_ORDER_CHUNK histories counting-
+ * sorted by sample count, so that the 32 histories of a warp run about the same
+ * number of samples (the rows and their slots do not depend on the order). */
+constexpr int MLP_ORDER_CHUNK = 4096;
+constexpr int MLP_ORDER_KEYS = 1024;
+__global__ void __launch_bounds__(1024) k_mlp_order(int64_t n, const int64_t* __restrict__ bound,
+                                                    uint32_t* __restrict__ order) {
+    __shared__ int cnt[MLP_ORDER_KEYS];
+    __shared__ int wsum[32];
+    const int64_t base = (int64_t)blockIdx.x * MLP_ORDER_CHUNK;
+    const int m = (int)(n - base < MLP_ORDER_CHUNK ? n - base : MLP_ORDER_CHUNK);
+    for (int k = threadIdx.x; k < MLP_ORDER_KEYS; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    constexpr int PER = MLP_ORDER_CHUNK / 1024;
+    int key[PER], rank[PER];
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+        const int t = threadIdx.x + r * 1024;
+        key[r] = -1;
+        if (t < m) {
+            const int64_t b = bound[base + t];
+            key[r] = (int)(b < MLP_ORDER_KEYS - 1 ? b : MLP_ORDER_KEYS - 1);
+            rank[r] = atomicAdd(&cnt[key[r]], 1);
+        }
+    }
+    __syncthreads();
+    /* exclusive scan of the 1024 bucket counts, one per thread */
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v = cnt[threadIdx.x], incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int s = wsum[lane], si = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= o) si += y;
+        }
+        wsum[lane] = si - s;
+    }
+    __syncthreads();
+    const int excl = incl - v + wsum[w];
+    __syncthreads();
+    cnt[threadIdx.x] = excl;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < PER; ++r)
+        if (key[r] >= 0) order[base + cnt[key[r]] + rank[r]] = (uint32_t)(base + threadIdx.x + r * 1024);
+}
+
 /* Fills the row slot of each history.  A sample within `margin` of a voxel
  * face has two candidate voxels; when they are exactly the previous row entry
  * and the (certain) next sample's voxel, either choice gives the same row
@@ -798,7 +852,8 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
  * uncertain sample gets a placeholder entry, is queued for k_mlp_fix, and the
  * next sample is written unconditionally; k_mlp_dedupe then drops the repeats
  * around the resolved entries.  With exact != 0 every sample is binary64. */
-__global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const MlpRec* __restrict__ rec,
+__global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const uint32_t* __restrict__ order,
+                                                  const MlpRec* __restrict__ rec,
                                                   const uint32_t* __restrict__ first_voxel,
                                                   const float* __restrict__ x_entry, const float* __restrict__ y_entry,
                                                   const MlpTableEntry* __restrict__ tab, int kmax, float margin,
@@ -809,6 +864,7 @@ __global__ void __launch_bounds__(128) k_mlp_fast(DevGeom g, int64_t n, const Ml
                                                   unsigned long long* __restrict__ flags) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (order) i = order[i];
     const MlpRec& R = rec[i];
     const double u_2 = R.m.u_2;
     const int K = dev_sample_count(tab, kmax, u_2, g.mlp_u_step);
@@ -966,15 +1022,15 @@ __device__ double dev_chord(const DevGeom& g, double abs_angle_t, double abs_ang
 /* bf16: the chord length rounded to bfloat16 (round to nearest even), the value
  * a bf16 store holds; it then enters the row norm and the DROP updates. */
 __global__ void k_row_norms(DevGeom g, int64_t n, HistView h, const int* __restrict__ len, float* __restrict__ chord,
-                            double* __restrict__ inv_norm, int bf16) {
+                            float* __restrict__ row_scale, int bf16) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double ae = h.xy_entry_angle[i], ax = h.xy_exit_angle[i], ze = h.xz_entry_angle[i], zx = h.xz_exit_angle[i];
     double c = dev_chord(g, (ae + ax) / 2.0, (ze + zx) / 2.0);
     if (bf16) c = (double)__bfloat162float(__float2bfloat16_rn((float)c));
     chord[i] = (float)c;
-    double nn = (double)len[i];
-    inv_norm[i] = 1.0 / ((c * c) * nn);
+    /* ||a_i||^2 = c^2 len; the DROP update is lambda res c / ||a_i||^2 = lambda res row_scale */
+    row_scale[i] = (float)(1.0 / (c * (double)len[i]));
 }
 
 /* Exclusive scan of int64 lengths into offsets[0..n]: per-tile sums, a scan of
@@ -1071,7 +1127,7 @@ pct_status pct_stage_row_norms(pct_ctx* c) {
     HistView h = c->view(c->h);
     ++c->launches;
     k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(), c->chord.as<float>(),
-                                                             c->inv_norm.as<double>(), c->cfg.chord_bf16);
+                                                             c->row_scale.as<float>(), c->cfg.chord_bf16);
     PCT_CUDA(cudaGetLastError());
     return PCT_OK;
 }
@@ -1115,7 +1171,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
     PCT_TRY(c->row_offsets.alloc(sizeof(int64_t) * (n + 1)));
     PCT_TRY(c->row_len.alloc(sizeof(int) * (n > 0 ? n : 1)));
     PCT_TRY(c->chord.alloc(sizeof(float) * (n > 0 ? n : 1)));
-    PCT_TRY(c->inv_norm.alloc(sizeof(double) * (n > 0 ? n : 1)));
+    PCT_TRY(c->row_scale.alloc(sizeof(float) * (n > 0 ? n : 1)));
     int kmax = 0;
     PCT_TRY(ensure_mlp_table(c, &kmax));
     int64_t bound_total = 0;
@@ -1138,9 +1194,17 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (bound_total > 0 ? bound_total : 1)));
         const int exact = c->cfg.mlp_exact != 0;
         const float margin = (float)c->cfg.mlp_face_margin;
+        uint32_t* order = nullptr;
+        if (n <= (int64_t)0xffffffffu) {
+            PCT_TRY(c->mlp_order.alloc(sizeof(uint32_t) * n));
+            order = c->mlp_order.as<uint32_t>();
+            ++c->launches;
+            k_mlp_order<<<(unsigned)((n + MLP_ORDER_CHUNK - 1) / MLP_ORDER_CHUNK), 1024, 0, c->stream>>>(
+                n, c->mlp_bound.as<int64_t>(), order);
+        }
         ++c->launches;
         k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
-            c->dg, n, rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
+            c->dg, n, order, rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
             c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(), c->mlp_queue.as<MlpDeferred>(),
             queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
         c->launches += 2;
@@ -1152,7 +1216,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
                                                      c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels, flags);
         ++c->launches;
         k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(),
-                                                                 c->chord.as<float>(), c->inv_norm.as<double>(),
+                                                                 c->chord.as<float>(), c->row_scale.as<float>(),
                                                                  c->cfg.chord_bf16);
         PCT_CUDA(cudaGetLastError());
     }

@@ -58,10 +58,10 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_rows(int64_t start, int64_t e
                                                         const float* __restrict__ wepl, float lambda,
                                                         const float* __restrict__ x, float* __restrict__ upd,
                                                         uint32_t nv, double* __restrict__ resid) {
-    __shared__ double sres[NA_WARPS];
+    __shared__ float sres[NA_WARPS];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t i = start + (int64_t)blockIdx.x * NA_WARPS + w;
-    double r2 = 0.0;
+    float r2 = 0.0f;
     if (i < end) {
         int64_t a = off[i], b = off[i + 1];
         float dot = 0.0f;
@@ -70,10 +70,9 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_rows(int64_t start, int64_t e
             if (v < nv) dot += x[v];
         }
         for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-        double c = chord[i];
-        double res = (double)wepl[i] - c * (double)dot;
-        double inv_norm = 1.0 / ((c * c) * (double)(b - a));
-        float value = (float)(c * res * inv_norm * (double)lambda);
+        const float c = chord[i];
+        const float res = fmaf(-c, dot, wepl[i]);
+        const float value = (res / (c * (float)(b - a))) * lambda; /* lambda res c / (c^2 len) */
         for (int64_t p = a + lane; p < b; p += 32) {
             uint32_t v = rows[p];
             if (v < nv) atomicAdd(upd + v, value);
@@ -83,9 +82,9 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_rows(int64_t start, int64_t e
     if (lane == 0) sres[w] = r2;
     __syncthreads();
     if (threadIdx.x == 0 && resid) {
-        double s = 0.0;
+        float s = 0.0f;
         for (int k = 0; k < NA_WARPS; ++k) s += sres[k];
-        if (s != 0.0) atomicAdd(resid, s);
+        if (s != 0.0f) atomicAdd(resid, (double)s);
     }
 }
 

@@ -95,6 +95,9 @@ DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g) {
     /* exact for n < 2^31 since 64 >= 31 + log2(d) */
     d.div_c = g.columns > 1 ? (~0ull) / (unsigned long long)g.columns + 1ull : 0ull;
     d.div_r = g.rows > 1 ? (~0ull) / (unsigned long long)g.rows + 1ull : 0ull;
+    d.fx0 = (float)g.x_zero; d.fy0 = (float)g.y_zero; d.fz0 = (float)g.z_zero;
+    d.fvw = (float)g.voxel_width; d.fvh = (float)g.voxel_height; d.fvt = (float)g.voxel_thickness;
+    d.fivw = 1.0f / d.fvw; d.fivh = 1.0f / d.fvh; d.fivt = 1.0f / d.fvt; /* IEEE quotients, as on the device */
     return d;
 }
 
@@ -296,8 +299,8 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->filter_taps, &c->filter_scale, &c->trig_gantry, &c->trig_bins, &c->err_flags,
                      &c->sc_hull, &c->msc_counts, &c->sm_counts, &c->msc_hull, &c->sm_hull, &c->fbp_image,
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
-                     &c->rows, &c->chord, &c->inv_norm, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
-                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows,
+                     &c->rows, &c->chord, &c->row_scale, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
+                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order,
                      &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm};
     for (DevBuf* b : all) b->release();
     c->td.release();

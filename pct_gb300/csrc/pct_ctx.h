@@ -78,6 +78,9 @@ struct DevGeom {
     double t_bin_size, v_bin_size, angular_bin_size, gantry_angle_interval, source_radius, slice_thickness;
     int brick; /* MLP rows and the DROP iterate use the 4x2x1 brick voxel order (see pct_device.cuh) */
     unsigned long long div_c, div_r; /* ceil(2^64 / COLUMNS), ceil(2^64 / ROWS): q = umulhi64(n, m) */
+    /* binary32 copies for the binary32 walks and MLP samples (a conversion in the
+     * kernel would run on the FP64 pipe at every use) */
+    float fx0, fy0, fz0, fvw, fvh, fvt, fivw, fivh, fivt;
 };
 
 enum Stage {
@@ -133,8 +136,8 @@ struct pct_ctx {
     DevBuf x_brick;                /* the iterate in brick order while DROP runs */
 
     /* MLP rows and DROP */
-    DevBuf row_offsets, row_len, rows, chord, inv_norm, mlp_table;  /* row_offsets: start of each row's slot */
-    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows;             /* MLP row generation scratch */
+    DevBuf row_offsets, row_len, rows, chord, row_scale, mlp_table;  /* row_offsets: start of each row's slot */
+    DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows, mlp_order;  /* MLP row generation scratch */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
     DevBuf block_norm;             /* per DROP block: sum of c^2 per voxel (robust variant) */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
