@@ -735,19 +735,19 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     float d = (f.u2_hi - te.u1_hi) + (f.u2_lo - te.u1_lo);
     float k2 = 13.6f * (1.0f + 0.038f * (__logf(d) - lnX0));
     float c2 = k2 * k2 * (1.0f / 36.08f);
-    float Q1 = b[5] * (1.0f / 6), Q2 = b[5] * (1.0f / 7), Q3 = b[5] * (1.0f / 8);
-    Q1 = fmaf(Q1, d, b[4] * (1.0f / 5)); Q2 = fmaf(Q2, d, b[4] * (1.0f / 6)); Q3 = fmaf(Q3, d, b[4] * (1.0f / 7));
-    Q1 = fmaf(Q1, d, b[3] * (1.0f / 4)); Q2 = fmaf(Q2, d, b[3] * (1.0f / 5)); Q3 = fmaf(Q3, d, b[3] * (1.0f / 6));
-    Q1 = fmaf(Q1, d, b[2] * (1.0f / 3)); Q2 = fmaf(Q2, d, b[2] * (1.0f / 4)); Q3 = fmaf(Q3, d, b[2] * (1.0f / 5));
-    Q1 = fmaf(Q1, d, b[1] * (1.0f / 2)); Q2 = fmaf(Q2, d, b[1] * (1.0f / 3)); Q3 = fmaf(Q3, d, b[1] * (1.0f / 4));
-    Q1 = fmaf(Q1, d, b[0]);              Q2 = fmaf(Q2, d, b[0] * (1.0f / 2)); Q3 = fmaf(Q3, d, b[0] * (1.0f / 3));
+    /* the terms p_m = b_m d^m once, then each moment as a fixed-weight sum of them */
+    const float d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
+    const float p0 = b[0], p1 = b[1] * d, p2 = b[2] * d2, p3 = b[3] * d3, p4 = b[4] * d4, p5 = b[5] * d5;
+#define PCT_WSUM(w0, w1, w2, w3, w4, w5) \
+    fmaf(p5, (w5), fmaf(p4, (w4), fmaf(p3, (w3), fmaf(p2, (w2), fmaf(p1, (w1), p0 * (w0))))))
+    float Q1 = PCT_WSUM(1.0f, 1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6);
+    float Q2 = PCT_WSUM(1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6, 1.0f / 7);
+    float Q3 = PCT_WSUM(1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6, 1.0f / 7, 1.0f / 8);
     /* E1 = Q1 - Q2 (weights 1/((m+1)(m+2))), E2 = Q1 - 2 Q2 + Q3, E3 = Q2 - Q3, each summed directly */
-    float E1 = b[5] * (1.0f / 42), E2 = b[5] * (2.0f / 336), E3 = b[5] * (1.0f / 56);
-    E1 = fmaf(E1, d, b[4] * (1.0f / 30)); E2 = fmaf(E2, d, b[4] * (2.0f / 210)); E3 = fmaf(E3, d, b[4] * (1.0f / 42));
-    E1 = fmaf(E1, d, b[3] * (1.0f / 20)); E2 = fmaf(E2, d, b[3] * (2.0f / 120)); E3 = fmaf(E3, d, b[3] * (1.0f / 30));
-    E1 = fmaf(E1, d, b[2] * (1.0f / 12)); E2 = fmaf(E2, d, b[2] * (2.0f / 60));  E3 = fmaf(E3, d, b[2] * (1.0f / 20));
-    E1 = fmaf(E1, d, b[1] * (1.0f / 6));  E2 = fmaf(E2, d, b[1] * (2.0f / 24));  E3 = fmaf(E3, d, b[1] * (1.0f / 12));
-    E1 = fmaf(E1, d, b[0] * (1.0f / 2));  E2 = fmaf(E2, d, b[0] * (2.0f / 6));   E3 = fmaf(E3, d, b[0] * (1.0f / 6));
+    float E1 = PCT_WSUM(1.0f / 2, 1.0f / 6, 1.0f / 12, 1.0f / 20, 1.0f / 30, 1.0f / 42);
+    float E2 = PCT_WSUM(2.0f / 6, 2.0f / 24, 2.0f / 60, 2.0f / 120, 2.0f / 210, 2.0f / 336);
+    float E3 = PCT_WSUM(1.0f / 6, 1.0f / 12, 1.0f / 20, 1.0f / 30, 1.0f / 42, 1.0f / 56);
+#undef PCT_WSUM
     float D = fmaf(Q3, Q1, -Q2 * Q2);
     /* approximate reciprocals (2 ulp): far inside the face margin that certifies each voxel */
     float inv = __fdividef(1.0f, c2 * D);
@@ -966,25 +966,43 @@ __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __rest
     }
 }
 
-/* Drops consecutive repeats in the rows that had queued samples. */
-__global__ void k_mlp_dedupe(int64_t rows_cap, const int64_t* __restrict__ fix_rows,
-                             const int64_t* __restrict__ row_start, int* __restrict__ row_len,
-                             uint32_t* __restrict__ rows, uint32_t nv, unsigned long long* __restrict__ flags) {
+/* Drops consecutive repeats in the rows that had queued samples, one warp per
+ * row.  An entry is kept when it differs from the entry before it (the last
+ * kept value always equals that entry), and kept entries are compacted in
+ * place: each 32-entry chunk is read into registers before any lane writes,
+ * and writes never pass the chunk being read. */
+__global__ void __launch_bounds__(256) k_mlp_dedupe(int64_t rows_cap, const int64_t* __restrict__ fix_rows,
+                                                    const int64_t* __restrict__ row_start, int* __restrict__ row_len,
+                                                    uint32_t* __restrict__ rows, uint32_t nv,
+                                                    unsigned long long* __restrict__ flags) {
     int64_t count = (int64_t)flags[ERR_MLP_FIXROWS];
     if (count > rows_cap) count = rows_cap;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < count; r += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = fix_rows[r];
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < count; r += warps) {
+        const int64_t i = fix_rows[r];
         uint32_t* row = rows + row_start[i];
-        int len = row_len[i], w = 1, outside = row[0] >= nv;
-        for (int j = 1; j < len; ++j) {
-            uint32_t v = row[j];
-            if (v != row[w - 1]) {
-                row[w++] = v;
-                outside += v >= nv;
-            }
+        const int len = row_len[i];
+        int w = 0, outside = 0;
+        uint32_t last = 0; /* entry base - 1 */
+        for (int base = 0; base < len; base += 32) {
+            const int j = base + lane;
+            const uint32_t v = j < len ? row[j] : 0u;
+            uint32_t before = __shfl_up_sync(0xffffffffu, v, 1);
+            if (lane == 0) before = last;
+            last = __shfl_sync(0xffffffffu, v, 31);
+            const bool keep = j < len && (j == 0 || v != before);
+            const unsigned kb = __ballot_sync(0xffffffffu, keep);
+            outside += __popc(__ballot_sync(0xffffffffu, keep && v >= nv));
+            __syncwarp();
+            if (keep) row[w + __popc(kb & ((1u << lane) - 1u))] = v;
+            w += __popc(kb);
+            __syncwarp();
         }
-        row_len[i] = w;
-        if (outside) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
+        if (lane == 0) {
+            row_len[i] = w;
+            if (outside) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
+        }
     }
 }
 
@@ -1211,7 +1229,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         k_mlp_fix<<<4 * 152, 128, 0, c->stream>>>(c->dg, rec, c->mlp_table.as<MlpTableEntry>(),
                                                   c->mlp_queue.as<MlpDeferred>(), queue_cap, flags,
                                                   c->rows.as<uint32_t>());
-        k_mlp_dedupe<<<2 * 152, 128, 0, c->stream>>>(n, c->mlp_fix_rows.as<int64_t>(),
+        k_mlp_dedupe<<<8 * 152, 256, 0, c->stream>>>(n, c->mlp_fix_rows.as<int64_t>(),
                                                      c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
                                                      c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels, flags);
         ++c->launches;
