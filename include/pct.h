@@ -312,6 +312,36 @@ pct_status pct_read_mlp_paths(pct_ctx* ctx, const char* path);
 pct_status pct_write_image(pct_ctx* ctx, pct_array which, const char* path);
 pct_status pct_read_image(pct_ctx* ctx, const char* path);
 
+/* Sharded DROP: the rows of every DROP block split over several contexts
+ * (ranks), with one elementwise sum over the ranks per block -- the
+ * partitioning of a block's histories across GPUs that block_update_GPU's
+ * independence within a block allows (.cu:5774-5841, .cu:6803-6844).
+ *
+ * pct_select_shard (after pct_collect_mlp_endpoints, before pct_mlp_rows)
+ * keeps the reconstruction histories i with i % num_shards == shard and makes
+ * the block size block_size / num_shards (block_size must be a multiple of
+ * num_shards), so that local block k holds this rank's share of global block
+ * k; every rank keeps the global number of blocks, some possibly empty.
+ *
+ * With an all-reduce callback set, pct_drop (scatter or sorted form; the tiled
+ * form falls back to scatter) synchronises the context stream and calls
+ * fn(user, data, count, dtype, on_device) for: the DROP diagonal counts of
+ * all blocks once (PCT_DT_U32, num_blocks * NUM_VOXELS), the sum of squared
+ * WEPL once (PCT_DT_F64, 1), then in every iteration each block's update
+ * image (PCT_DT_F32, NUM_VOXELS) before it is applied and the iteration's
+ * squared residual (PCT_DT_F64, 1); with the ROBUST2 variant also the
+ * per-voxel c^2 sums once (PCT_DT_F32, num_blocks * NUM_VOXELS).  `data` is
+ * device memory of the context's device (on_device = 1); the callback returns
+ * 0 with `data` replaced by the elementwise sum over the ranks and all its
+ * own device work complete.  Every rank makes the same sequence of calls.
+ * fn = NULL restores the single-context DROP. */
+enum { PCT_DT_F32 = 0, PCT_DT_U32 = 1, PCT_DT_F64 = 2 };
+typedef int (*pct_allreduce_fn)(void* user, void* data, int64_t count, int dtype, int on_device);
+pct_status pct_set_allreduce(pct_ctx* ctx, pct_allreduce_fn fn, void* user);
+pct_status pct_select_shard(pct_ctx* ctx, int shard, int num_shards);
+/* cudaMemcpy with the direction taken from the pointers (for callbacks). */
+pct_status pct_memcpy(void* dst, const void* src, int64_t bytes);
+
 pct_status pct_config_default(pct_config* cfg);
 pct_status pct_geometry_from_config(const pct_config* cfg, pct_geometry* geo);
 const char* pct_last_error(void);

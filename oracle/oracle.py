@@ -27,6 +27,10 @@ def _p(a):
     return C.c_void_p(a.ctypes.data) if a is not None else None
 
 
+# pct_allreduce_fn (include/pct.h): user, data, count, dtype, on_device -> 0 on success
+ALLREDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int)
+
+
 def load():
     global _lib
     if _lib is None:
@@ -42,6 +46,8 @@ def load():
                                           C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p]
         _lib.ora_drop_mt.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_int]
+        _lib.ora_drop_shard.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p, ALLREDUCE_FN, C.c_void_p]
     return _lib
 
 
@@ -196,6 +202,17 @@ def drop(cfg, offsets, rows, chord, wepl, x0, iterations, block_size, lam, threa
         rc = load().ora_drop(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord), _p(w), iterations,
                              block_size, C.c_double(lam), _p(x))
     assert rc == 0
+    return x
+
+
+def drop_shard(cfg, offsets, rows, chord, wepl, x0, iterations, block_size, num_blocks, lam, allreduce):
+    """ora_drop on one shard of the rows; allreduce(user, data, count, dtype, on_device) -> 0 sums over ranks."""
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    w = np.ascontiguousarray(wepl, np.float32)
+    fn = ALLREDUCE_FN(allreduce)
+    rc = load().ora_drop_shard(_cfgp(cfg), C.c_int64(len(chord)), _p(offsets), _p(rows), _p(chord), _p(w),
+                               iterations, block_size, num_blocks, C.c_double(lam), _p(x), fn, None)
+    assert rc == 0, rc
     return x
 
 

@@ -1001,6 +1001,55 @@ int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uin
     return 0;
 }
 
+/* ora_drop over one shard: the same block update (block_update_GPU
+ * .cu:5774-5841 / DROP_blocks .cu:8023-8043) on this rank's rows of block k,
+ * the sums over the ranks, then DROP_update (.cu:8044-8055). */
+int ora_drop_shard(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
+                   const float* wepl, int iterations, int block_size, int num_blocks, double lambda, double* x,
+                   pct_allreduce_fn fn, void* user) {
+    pct_geometry g;
+    if (pct_geometry_derive(cfg, &g) || block_size < 1 || num_blocks < 0 || !fn) return 1;
+    const int nv = g.num_voxels;
+    double* upd = (double*)calloc((size_t)nv, sizeof(double));
+    uint32_t* cnt = (uint32_t*)calloc((size_t)nv, sizeof(uint32_t));
+    if (!upd || !cnt) { free(upd); free(cnt); return 2; }
+    int rc = 0;
+    for (int it = 0; it < iterations && !rc; ++it) {
+        for (int k = 0; k < num_blocks && !rc; ++k) {
+            int64_t start = (int64_t)k * block_size;
+            if (start > n) start = n;
+            int64_t end = start + block_size < n ? start + block_size : n;
+            for (int64_t i = start; i < end; ++i) {
+                double c = chord[i];
+                int64_t a = offsets[i], b = offsets[i + 1];
+                double dot = 0.0;
+                for (int64_t j = a; j < b; ++j)
+                    if (rows[j] < (uint32_t)nv) dot += x[rows[j]];
+                dot *= c;
+                double aa = (c * c) * (double)(b - a);
+                double value = c * ((wepl[i] - dot) / aa) * lambda;
+                for (int64_t j = a; j < b; ++j)
+                    if (rows[j] < (uint32_t)nv) {
+                        cnt[rows[j]] += 1;
+                        upd[rows[j]] += value;
+                    }
+            }
+            if (fn(user, upd, nv, PCT_DT_F64, 0) || fn(user, cnt, nv, PCT_DT_U32, 0)) {
+                rc = 3;
+                break;
+            }
+            for (int v = 0; v < nv; ++v) {
+                if (cnt[v] > 0) x[v] += upd[v] / cnt[v];
+                upd[v] = 0.0;
+                cnt[v] = 0;
+            }
+        }
+    }
+    free(upd);
+    free(cnt);
+    return rc;
+}
+
 /* DROP variants of the reference's CPU reconstruction, binary64:
  *   variant 1  DROP_blocks_red (.cu:7998-8021): each entry's update is
  *              c lambda r / (||a||^2 + psi_j), psi_j = ((1 - x_j) eta) psi_sign,

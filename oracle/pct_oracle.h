@@ -89,6 +89,15 @@ double ora_effective_chord_length(const pct_config* cfg, double abs_angle_t, dou
 int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
              const float* wepl, int iterations, int block_size, double lambda, double* x);
 
+/* a16-a19 as one shard of a sharded DROP: `n` local rows, this rank's share of
+ * every global block in order (local block size block_size, num_blocks global
+ * blocks, some possibly empty here); each block's binary64 update and counts
+ * are summed over the ranks by fn (PCT_DT_F64 / PCT_DT_U32, host memory,
+ * on_device = 0) before x += update / s. */
+int ora_drop_shard(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
+                   const float* wepl, int iterations, int block_size, int num_blocks, double lambda, double* x,
+                   pct_allreduce_fn fn, void* user);
+
 /* a16-a19 variants: 1 DROP_blocks_red, 2 DROP_blocks_robust2 + DROP_update_robust2 (0 = ora_drop). */
 int ora_drop_variant(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows,
                      const double* chord, const float* wepl, int iterations, int block_size, double lambda,

@@ -72,6 +72,11 @@ _STRUCTS = [(0, Config), (1, Geometry), (2, PhantomObject), (3, ScanParams)]
 _lib = None
 
 
+# pct_allreduce_fn: (user, data, count, dtype, on_device) -> 0 on success
+ALLREDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int)
+PCT_DT_F32, PCT_DT_U32, PCT_DT_F64 = 0, 1, 2
+
+
 def load():
     """Returns the loaded library; raises if it was never built."""
     global _lib

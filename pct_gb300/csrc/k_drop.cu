@@ -306,15 +306,44 @@ __global__ void k_image_from_brick(DevGeom g, const float* __restrict__ brk, flo
 }  // namespace
 
 /* Per-block voxel counts for the scatter form. */
-static pct_status build_scatter(pct_ctx* c) {
-    const int64_t n = c->h.n;
+/* Number of DROP blocks: of this context's rows, or of the global rows when the
+ * rows are one shard of a sharded DROP (every rank runs every block). */
+static int drop_num_blocks(const pct_ctx* c) {
     const int64_t B = c->cfg.block_size;
+    if (c->num_shards > 1) {
+        const int64_t Bg = B * c->num_shards;
+        return (int)((c->shard_total + Bg - 1) / Bg);
+    }
+    return (int)((c->h.n + B - 1) / B);
+}
+
+/* Rows [s, e) of block k (empty past the end of a shard). */
+static void drop_block_range(const pct_ctx* c, int k, int64_t* s, int64_t* e) {
+    const int64_t n = c->h.n, B = c->cfg.block_size;
+    const int64_t a = (int64_t)k * B;
+    *s = a < n ? a : n;
+    *e = a + B < n ? a + B : n;
+    if (*e < *s) *e = *s;
+}
+
+/* Sum over the ranks of a sharded DROP (no-op without a callback). */
+static pct_status drop_allreduce(pct_ctx* c, void* data, int64_t count, int dtype) {
+    if (!c->allreduce) return PCT_OK;
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    const int rc = c->allreduce(c->allreduce_user, data, count, dtype, 1);
+    if (rc != 0) return pct_fail(PCT_ERR_ARGUMENT, "sharded DROP: the all-reduce callback returned %d", rc);
+    return PCT_OK;
+}
+
+static pct_status build_scatter(pct_ctx* c) {
     const int nv = c->geo.num_voxels;
-    int nb = (int)((n + B - 1) / B);
+    int nb = drop_num_blocks(c);
     PCT_TRY(c->block_diag.alloc(sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1)));
     PCT_CUDA(cudaMemsetAsync(c->block_diag.p, 0, sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
     for (int k = 0; k < nb; ++k) {
-        int64_t s = k * B, e = s + B < n ? s + B : n;
+        int64_t s, e;
+        drop_block_range(c, k, &s, &e);
+        if (e == s) continue;
         ++c->launches;
         k_block_counts<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
             s, e, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), (uint32_t)nv,
@@ -324,7 +353,9 @@ static pct_status build_scatter(pct_ctx* c) {
         PCT_TRY(c->block_norm.alloc(sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1)));
         PCT_CUDA(cudaMemsetAsync(c->block_norm.p, 0, sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
         for (int k = 0; k < nb; ++k) {
-            int64_t s = k * B, e = s + B < n ? s + B : n;
+            int64_t s, e;
+            drop_block_range(c, k, &s, &e);
+            if (e == s) continue;
             ++c->launches;
             k_block_norms<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
                 s, e, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), c->rows.as<uint32_t>(), c->chord.as<float>(),
@@ -332,6 +363,11 @@ static pct_status build_scatter(pct_ctx* c) {
         }
     }
     PCT_CUDA(cudaGetLastError());
+    if (nb > 0) {
+        PCT_TRY(drop_allreduce(c, c->block_diag.p, (int64_t)nv * nb, PCT_DT_U32));
+        if (c->cfg.drop_variant == PCT_DROP_ROBUST2)
+            PCT_TRY(drop_allreduce(c, c->block_norm.p, (int64_t)nv * nb, PCT_DT_F32));
+    }
     c->num_blocks = nb;
     c->drop_mode = PCT_DROP_SCATTER;
     c->drop_launches_per_iter = 2 * nb;
@@ -342,10 +378,9 @@ static pct_status build_scatter(pct_ctx* c) {
 /* Bin order of every block's rows for the sorted form (counts as in the scatter form). */
 static pct_status build_sorted(pct_ctx* c) {
     const int64_t n = c->h.n;
-    const int64_t B = c->cfg.block_size;
     const uint32_t nkeys = (uint32_t)c->geo.num_bins;
     const int tiles = (int)((nkeys + SCAN_TILE - 1) / SCAN_TILE);
-    int nb = (int)((n + B - 1) / B);
+    int nb = drop_num_blocks(c);
     PCT_TRY(c->drop_perm.alloc(sizeof(uint32_t) * (n > 0 ? n : 1)));
     PCT_TRY(c->drop_sort.alloc(sizeof(uint32_t) * ((size_t)2 * nkeys + tiles)));
     uint32_t* cnt = c->drop_sort.as<uint32_t>();
@@ -354,7 +389,9 @@ static pct_status build_sorted(pct_ctx* c) {
     const int32_t* bin = c->h.bin_num.as<int32_t>();
     uint32_t* perm = c->drop_perm.as<uint32_t>();
     for (int k = 0; k < nb; ++k) {
-        int64_t s = k * B, e = s + B < n ? s + B : n;
+        int64_t s, e;
+        drop_block_range(c, k, &s, &e);
+        if (e == s) continue;
         PCT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * nkeys, c->stream));
         c->launches += 5;
         k_sort_count<<<pct_grid_for(e - s, 256), 256, 0, c->stream>>>(s, e, bin, nkeys, cnt);
@@ -381,42 +418,69 @@ static unsigned drop_rows_grid(pct_ctx* c, int64_t rows, const void* fn) {
     return (unsigned)(need < cap ? (need > 0 ? need : 1) : cap);
 }
 
+/* The row pass of block k (scatter and sorted forms): x_update and the
+ * residual accumulator; returns the number of launches. */
+static int enqueue_block_rows(pct_ctx* c, int k, double* resid) {
+    int64_t s, e;
+    drop_block_range(c, k, &s, &e);
+    if (e == s) return 0;
+    const int nv = c->geo.num_voxels;
+    const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
+    float* xi = c->dg.brick ? c->x_brick.as<float>() : c->x.as<float>(); /* the rows' voxel order */
+    const int var = c->cfg.drop_variant;
+    const float eta = (float)c->cfg.eta, sgn = (float)c->cfg.psi_sign;
+    auto rows_kernel = var == PCT_DROP_RED ? k_drop_rows<1> : (var == PCT_DROP_ROBUST2 ? k_drop_rows<2> : k_drop_rows<0>);
+    const unsigned grid = drop_rows_grid(c, e - s, (const void*)rows_kernel);
+    rows_kernel<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
+                                                      c->rows.as<uint32_t>(), c->chord.as<float>(),
+                                                      c->row_scale.as<float>(), c->h.wepl.as<float>(), c->cfg.lambda,
+                                                      xi, c->x_update.as<float>(), (uint32_t)nv, resid, eta, sgn);
+    return 1;
+}
+
+/* x += x_update / s_j for block k (and x_update cleared); one launch. */
+static void enqueue_block_relax(pct_ctx* c, int k) {
+    const int nv = c->geo.num_voxels;
+    float* xi = c->dg.brick ? c->x_brick.as<float>() : c->x.as<float>();
+    const float eta = (float)c->cfg.eta, sgn = (float)c->cfg.psi_sign;
+    if (c->cfg.drop_variant == PCT_DROP_ROBUST2)
+        k_drop_relax_robust2<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(
+            nv, c->block_diag.as<uint32_t>() + (size_t)k * nv, c->block_norm.as<float>() + (size_t)k * nv, xi,
+            c->x_update.as<float>(), eta, sgn);
+    else if (nv % 4 == 0)
+        k_drop_relax4<<<pct_grid_for(nv / 4, 256), 256, 0, c->stream>>>(
+            nv / 4, reinterpret_cast<const uint4*>(c->block_diag.as<uint32_t>() + (size_t)k * nv),
+            reinterpret_cast<float4*>(xi), reinterpret_cast<float4*>(c->x_update.as<float>()));
+    else
+        k_drop_relax<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(nv, c->block_diag.as<uint32_t>() + (size_t)k * nv,
+                                                                   xi, c->x_update.as<float>());
+}
+
+/* One iteration of a sharded DROP: every block's update summed over the ranks
+ * before it is applied, then the iteration's squared residual; not captured
+ * (the callback runs on the host between the launches). */
+static pct_status run_iteration_sharded(pct_ctx* c, double* resid) {
+    for (int k = 0; k < c->num_blocks; ++k) {
+        c->launches += enqueue_block_rows(c, k, resid);
+        PCT_TRY(drop_allreduce(c, c->x_update.p, c->geo.num_voxels, PCT_DT_F32));
+        enqueue_block_relax(c, k);
+        ++c->launches;
+    }
+    PCT_CUDA(cudaGetLastError());
+    return drop_allreduce(c, resid, 1, PCT_DT_F64);
+}
+
 /* Enqueues one DROP iteration (all blocks) on the context stream. */
 static void enqueue_iteration(pct_ctx* c, double* resid) {
-    const int64_t n = c->h.n;
-    const int64_t B = c->cfg.block_size;
-    const int nv = c->geo.num_voxels;
     for (int k = 0; k < c->num_blocks; ++k) {
-        int64_t s = k * B, e = s + B < n ? s + B : n;
         if (c->drop_mode == PCT_DROP_TILED) {
             pct_drop_tiled_enqueue(c, k, resid);
             continue;
         }
-        const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
-        float* xi = c->dg.brick ? c->x_brick.as<float>() : c->x.as<float>(); /* the rows' voxel order */
-        const int var = c->cfg.drop_variant;
-        const float eta = (float)c->cfg.eta, sgn = (float)c->cfg.psi_sign;
-        auto rows_kernel = var == PCT_DROP_RED ? k_drop_rows<1> : (var == PCT_DROP_ROBUST2 ? k_drop_rows<2> : k_drop_rows<0>);
-        const unsigned grid = drop_rows_grid(c, e - s, (const void*)rows_kernel);
-        rows_kernel<<<grid, DROP_THREADS, 0, c->stream>>>(s, e, perm, c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
-                                                          c->rows.as<uint32_t>(), c->chord.as<float>(),
-                                                          c->row_scale.as<float>(), c->h.wepl.as<float>(),
-                                                          c->cfg.lambda, xi, c->x_update.as<float>(),
-                                                          (uint32_t)nv, resid, eta, sgn);
-        if (var == PCT_DROP_ROBUST2)
-            k_drop_relax_robust2<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(
-                nv, c->block_diag.as<uint32_t>() + (size_t)k * nv, c->block_norm.as<float>() + (size_t)k * nv, xi,
-                c->x_update.as<float>(), eta, sgn);
-        else if (nv % 4 == 0)
-            k_drop_relax4<<<pct_grid_for(nv / 4, 256), 256, 0, c->stream>>>(
-                nv / 4, reinterpret_cast<const uint4*>(c->block_diag.as<uint32_t>() + (size_t)k * nv),
-                reinterpret_cast<float4*>(xi), reinterpret_cast<float4*>(c->x_update.as<float>()));
-        else
-            k_drop_relax<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(nv, c->block_diag.as<uint32_t>() + (size_t)k * nv,
-                                                                       xi, c->x_update.as<float>());
+        enqueue_block_rows(c, k, resid);
+        enqueue_block_relax(c, k);
     }
 }
-
 static pct_status capture_iteration(pct_ctx* c, double* acc) {
     if (c->drop_graph_exec) return PCT_OK;
     cudaGraph_t graph = nullptr;
@@ -440,7 +504,7 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
         pct_drop_release_graph(c);
         c->td.release();
         const int form = c->cfg.drop_form;
-        if (form == PCT_DROP_TILED && pct_drop_tiled_fits(c)) {
+        if (form == PCT_DROP_TILED && !c->allreduce && c->num_shards == 1 && pct_drop_tiled_fits(c)) {
             PCT_TRY(pct_drop_tiled_build(c));
             const int64_t B = c->cfg.block_size;
             c->num_blocks = c->td.num_blocks;
@@ -470,7 +534,8 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
     double* d_res = c->drop_resid.as<double>();
     PCT_CUDA(cudaMemsetAsync(d_res, 0, sizeof(double) * (maxit + 2), c->stream));
     if (c->h.n > 0) k_wepl_norm<<<304, 256, 0, c->stream>>>(c->h.n, c->h.wepl.as<float>(), d_res + maxit + 1);
-    PCT_TRY(capture_iteration(c, d_res + maxit));
+    PCT_TRY(drop_allreduce(c, d_res + maxit + 1, 1, PCT_DT_F64));
+    if (!c->allreduce) PCT_TRY(capture_iteration(c, d_res + maxit));
     cudaEvent_t e0, e1;
     PCT_CUDA(cudaEventCreate(&e0));
     PCT_CUDA(cudaEventCreate(&e1));
@@ -478,8 +543,12 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
     int done = 0;
     double res_host[maxit + 2];
     for (int it = 0; it < iterations; ++it) {
-        PCT_CUDA(cudaGraphLaunch(c->drop_graph_exec, c->stream));
-        c->launches += c->drop_launches_per_iter;
+        if (c->allreduce) {
+            PCT_TRY(run_iteration_sharded(c, d_res + maxit));
+        } else {
+            PCT_CUDA(cudaGraphLaunch(c->drop_graph_exec, c->stream));
+            c->launches += c->drop_launches_per_iter;
+        }
         ++c->launches;
         k_store_resid<<<1, 1, 0, c->stream>>>(d_res + maxit, d_res + (it < maxit ? it : maxit - 1));
         ++done;

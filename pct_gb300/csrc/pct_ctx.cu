@@ -475,6 +475,57 @@ extern "C" pct_status pct_image_reconstruction(pct_ctx* c, pct_drop_stats* stats
     return pct_stage_drop(c, c->cfg.iterations, stats);
 }
 
+/* ---- sharded DROP ---- */
+
+__global__ void k_shard_keep(int64_t n, int shard, int num_shards, uint8_t* __restrict__ keep) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keep[i] = (uint8_t)(i % num_shards == shard);
+}
+
+extern "C" pct_status pct_set_allreduce(pct_ctx* c, pct_allreduce_fn fn, void* user) {
+    if (!c) return pct_fail(PCT_ERR_ARGUMENT, "null context");
+    c->allreduce = fn;
+    c->allreduce_user = fn ? user : nullptr;
+    c->diag_ready = 0; /* the diagonal counts are summed over the ranks when they are built */
+    pct_drop_release_graph(c);
+    return PCT_OK;
+}
+
+extern "C" pct_status pct_select_shard(pct_ctx* c, int shard, int num_shards) {
+    STAGE_ENTRY(c);
+    if (c->stage != ST_ENDPOINTS) return pct_fail(PCT_ERR_STATE, "pct_select_shard: call it after collect_mlp_endpoints");
+    if (c->num_shards != 1) return pct_fail(PCT_ERR_STATE, "pct_select_shard: the histories are already a shard");
+    if (num_shards < 1 || shard < 0 || shard >= num_shards)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_select_shard: shard %d of %d", shard, num_shards);
+    if (c->cfg.block_size % num_shards != 0)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_select_shard: block size %d is not a multiple of %d shards",
+                        c->cfg.block_size, num_shards);
+    const int64_t n = c->h.n;
+    c->shard_total = n;
+    if (num_shards > 1 && n > 0) {
+        PCT_TRY(c->tmp_missed.alloc(n));
+        uint8_t* keep = c->tmp_missed.as<uint8_t>();
+        ++c->launches;
+        k_shard_keep<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, shard, num_shards, keep);
+        PCT_CUDA(cudaGetLastError());
+        int64_t kept = 0;
+        PCT_TRY(pct_compact_histories(c, keep, n, &kept));
+        c->counts.reconstruction_histories = kept;
+    }
+    c->shard = shard;
+    c->num_shards = num_shards;
+    c->cfg.block_size /= num_shards;
+    c->diag_ready = 0;
+    return PCT_OK;
+}
+
+extern "C" pct_status pct_memcpy(void* dst, const void* src, int64_t bytes) {
+    if (bytes < 0 || (bytes > 0 && (!dst || !src))) return pct_fail(PCT_ERR_ARGUMENT, "pct_memcpy: bad arguments");
+    if (bytes == 0) return PCT_OK;
+    PCT_CUDA(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDefault));
+    return PCT_OK;
+}
+
 extern "C" pct_status pct_reset_iterate(pct_ctx* c) {
     STAGE_ENTRY(c);
     if (!c->x0.p || !c->x.p) return pct_fail(PCT_ERR_STATE, "pct_reset_iterate: no initial iterate");

@@ -148,6 +148,12 @@ struct pct_ctx {
     int64_t row_capacity = 0;
     int num_blocks = 0;
     int diag_ready = 0;
+    /* sharded DROP: all-reduce callback, this context's shard and the global
+     * number of reconstruction histories at pct_select_shard */
+    pct_allreduce_fn allreduce = nullptr;
+    void* allreduce_user = nullptr;
+    int shard = 0, num_shards = 1;
+    int64_t shard_total = 0;
     int drop_mode = 0;             /* built DROP form: PCT_DROP_TILED / _SORTED / _SCATTER */
     int drop_launches_per_iter = 0;
     TiledDrop td;

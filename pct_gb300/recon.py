@@ -73,6 +73,9 @@ def _declare(lib):
                  "pct_read_image"):
         getattr(lib, name).argtypes = [vp, C.c_char_p]
     lib.pct_write_image.argtypes = [vp, ci, C.c_char_p]
+    lib.pct_select_shard.argtypes = [vp, ci, ci]
+    lib.pct_set_allreduce.argtypes = [vp, _capi.ALLREDUCE_FN, vp]
+    lib.pct_memcpy.argtypes = [vp, vp, i64]
 
 
 class Reconstruction:
@@ -180,6 +183,15 @@ class Reconstruction:
 
     def reset_iterate(self):
         self._call("pct_reset_iterate")
+
+    def select_shard(self, shard, num_shards):
+        """Keeps this rank's share of every DROP block (pct_select_shard)."""
+        self._call("pct_select_shard", int(shard), int(num_shards))
+
+    def set_allreduce(self, fn):
+        """fn(user, data, count, dtype, on_device) -> 0 sums `data` over the ranks; None clears it."""
+        self._allreduce_fn = _capi.ALLREDUCE_FN(fn) if fn is not None else None
+        self._call("pct_set_allreduce", self._allreduce_fn if fn is not None else _capi.ALLREDUCE_FN(), None)
 
     def set_image(self, x):
         x = np.ascontiguousarray(x, dtype=np.float32)

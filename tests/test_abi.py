@@ -16,6 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions(header):
     text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"\btypedef\b[^;]*;", "", text)  # function-pointer types are not exports
     names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z_0-9]*\s*\**\s+\**([A-Za-z_][A-Za-z_0-9]*)\s*\(",
                        text, flags=re.M)
     return sorted(set(n for n in names if n not in ("if", "return", "sizeof")))
