@@ -275,7 +275,8 @@ def main():
     # ---- roofline of the dominant kernel ----------------------------------------------
     # One DROP iteration (the dominant part of a step: 12 of them per MLP pass).
     # Algorithmic bytes per recon history and iteration: 4 B WEPL + 8 B row start
-    # + 4 B chord + 8 B 1/||a||^2 + 4 B per row entry (voxel index); the image
+    # + 4 B row length + 4 B chord + 4 B row scale 1/(c |a_i|) + 4 B per row
+    # entry (voxel index); the image
     # gathers and update reductions stay in L2 and are not counted.  The launch
     # timed is one DROP iteration (all blocks: k_drop_rows + k_drop_relax per
     # block in the scatter form) with CUDA events on the context stream.
@@ -299,6 +300,49 @@ def main():
             traffic = tm["ratio_to_algorithmic"] * drop_bytes + tm["per_block_bytes"] * nblocks
     except Exception:
         pass
+
+    # MLP row generation, once per step: 48 B per recon history read (10 float
+    # endpoint values, WEPL, first voxel) + 4 B per row entry and 4 B row length
+    # written.
+    mlp_bytes = R * 52 + rows * 4
+    mlp_achieved = mlp_bytes / (mlp_s / a.steps) / 1e9
+
+    # ---- convergence: RSP error against the phantom per iteration (not timed) --------
+    # FBP x hull start, the same rows, one DROP iteration per call.  Regions: voxels
+    # whose 7x7 in-slice neighbourhood is one phantom material (3 voxels away from
+    # any boundary), grouped by material.  Reported: the RMS over materials of the
+    # relative error of the region mean RSP, and the per-voxel RMSE (noise included).
+    g = phantoms.geometry(cfg)
+    t3 = phantoms.voxelize(w).reshape(g.slices, g.rows, g.columns)
+    k = 3
+    pad = np.pad(t3, ((0, 0), (k, k), (k, k)), mode="edge")
+    same = t3 > 0
+    for dy in range(2 * k + 1):
+        for dx in range(2 * k + 1):
+            same &= pad[:, dy:dy + g.rows, dx:dx + g.columns] == t3
+    truth = t3.ravel()
+    roi = same.ravel()
+    mats = [(float(v), roi & (truth == v)) for v in np.unique(truth[roi])]
+    mats = [(v, m) for v, m in mats if m.sum() >= 200]
+
+    def errors(x):
+        region = [(x[m].mean() - v) / v for v, m in mats]
+        return (float(np.sqrt(np.mean(np.square(region))) * 100),
+                float(np.sqrt(np.mean((x[roi] - truth[roi]) ** 2)) * 100))
+
+    r.reset_iterate()
+    r.mlp_rows()
+    errs = [errors(r.array("X"))]
+    for _ in range(iters):
+        r.drop(1)
+        errs.append(errors(r.array("X")))
+    hit = next((k for k, e in enumerate(errs) if e[0] <= 0.5), None)
+    accuracy = {"region_mean_rsp_error_pct_per_iteration": [e[0] for e in errs],
+                "voxel_rsp_rmse_pct_per_iteration": [e[1] for e in errs],
+                "regions": "%d materials, %d voxels at least 3 voxels (in-slice) from a material boundary"
+                           % (len(mats), int(sum(m.sum() for _, m in mats))),
+                "start": "FBP x hull (iteration 0)",
+                "seconds_to_region_error_0.5pct": (mlp_s / a.steps + hit * drop_iter_s) if hit is not None else None}
 
     # ---- end to end through the public API with host buffers --------------------------
     pinned = torch.empty((13, n), dtype=torch.float32, pin_memory=True)
@@ -356,6 +400,10 @@ def main():
                          "frac": achieved / hbm_peak, "traffic": traffic,
                          "algorithmic_bytes": drop_bytes,
                          "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"},
+            "roofline_mlp": {"bound": "hbm", "kernel": "MLP row generation (k_mlp_bound .. k_row_norms)",
+                             "achieved": mlp_achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": mlp_achieved / hbm_peak, "algorithmic_bytes": mlp_bytes},
+            "accuracy": accuracy,
             "cpu_baseline": cpu_b, "gpu_launches": launches, "clocks": clocks,
         }
         print(json.dumps(out))
