@@ -5,8 +5,9 @@
  * reference's block loop .cu:6803-6844) one launch does block_update_GPU
  * (.cu:5774-5841) without the MLP: the dot of every row with the iterate at
  * the start of the block, the update value c * lambda * (b - c sum x) / ||a||^2
- * with ||a||^2 in binary64, its addition to every voxel of the row, and the
- * binary64 squared residual; a second launch is image_update_GPU
+ * (binary32, with 1 / (c |a|) rounded once from binary64), its addition to every
+ * voxel of the row, and the squared residual (summed in binary64 per CTA); a
+ * second launch is image_update_GPU
  * (.cu:5900-5938): x += x_update / s_j with s_j the number of block row
  * entries in voxel j (the DROP diagonal weight).  s_j depends only on the
  * rows and the block split, so it is counted once per set of rows instead of
