@@ -332,10 +332,12 @@ __device__ __forceinline__ bool step32(const DevGeom& g, const WalkLine& L, cons
 
 /* Same walk and image updates as k_hull_walk. */
 __global__ void __launch_bounds__(256) k_hull_walk_fast(DevGeom g, int kind, double threshold, int64_t n,
+                                                        const uint32_t* __restrict__ order,
                                                         const uint8_t* __restrict__ missed, HistView h,
                                                         int* __restrict__ img, unsigned long long* __restrict__ flags) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (order) i = order[i];
     float wepl = h.wepl[i];
     int use = kind == 2 ? (wepl >= threshold) : (wepl <= threshold);
     if (missed[i] || !use) return;
@@ -539,6 +541,23 @@ static pct_status ensure_hull_images(pct_ctx* c) {
     return PCT_OK;
 }
 
+/* Work estimate of one hull walk for the launch order: the voxel boundaries
+ * between entry and exit (0 for histories the walk skips). */
+__global__ void k_walk_key(DevGeom g, int kind, double threshold, int64_t n, const uint8_t* __restrict__ missed,
+                           HistView h, uint32_t* __restrict__ key) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float wepl = h.wepl[i];
+    const int use = kind == 2 ? (wepl >= threshold) : (wepl <= threshold);
+    uint32_t k = 0;
+    if (!missed[i] && use) {
+        const float s = fabsf(h.x_exit[i] - h.x_entry[i]) * g.fivw + fabsf(h.y_exit[i] - h.y_entry[i]) * g.fivh +
+                        fabsf(h.z_exit[i] - h.z_entry[i]) * g.fivt;
+        k = s < 1.0e6f ? 1u + (uint32_t)s : 1000000u; /* NaN and huge: last bucket */
+    }
+    key[i] = k;
+}
+
 /* hull_detection (.cu:3265-3273) on the staged chunk c->h2[0, n). */
 pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed) {
     PCT_TRY(ensure_hull_images(c));
@@ -546,10 +565,27 @@ pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed) {
     unsigned grid = pct_grid_for(n, 256);
     unsigned long long* flags = c->err_flags.as<unsigned long long>();
     const bool exact = c->cfg.walk_exact != 0;
+    /* the binary32 walks run in order of walk length (warps of equal work) */
+    uint32_t* order = nullptr;
+    uint32_t* key = nullptr;
+    if (!exact && n > 0 && n <= (int64_t)0xffffffffu) {
+        PCT_TRY(c->walk_order.alloc(sizeof(uint32_t) * 2 * (size_t)n));
+        order = c->walk_order.as<uint32_t>();
+        key = order + n;
+    }
     auto walk = [&](const DevGeom& g, int kind, double thr, int64_t nn, const uint8_t* ms, const HistView& hv, int* img,
                     unsigned long long* fl) {
-        if (exact) k_hull_walk<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, img, fl);
-        else k_hull_walk_fast<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, img, fl);
+        if (exact) {
+            k_hull_walk<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, img, fl);
+            return;
+        }
+        if (order) {
+            c->launches += 2;
+            k_walk_key<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, key);
+            k_chunk_order<uint32_t><<<(unsigned)((nn + ORDER_CHUNK - 1) / ORDER_CHUNK), 1024, 0, c->stream>>>(nn, key,
+                                                                                                            order);
+        }
+        k_hull_walk_fast<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, order, ms, hv, img, fl);
     };
     if (c->cfg.sc_on) {
         ++c->launches;

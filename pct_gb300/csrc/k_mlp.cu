@@ -441,11 +441,27 @@ __device__ int dev_find_endpoint_fast(const DevGeom& g, const uint8_t* __restric
     return hit;
 }
 
-__global__ void __launch_bounds__(128) k_endpoints_fast(DevGeom g, int64_t n, const uint8_t* __restrict__ hull,
-                                                        HistView h, uint8_t* __restrict__ keep,
+/* Launch-order key of the endpoint walks: the distance of the history's line
+ * from the cylinder axis in the xy plane (walks from the cylinder to the hull
+ * have about the same length at the same distance), in 1/1000 of the radius. */
+__global__ void k_endpoint_key(DevGeom g, int64_t n, HistView h, uint32_t* __restrict__ key) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float xe = h.x_entry[i], ye = h.y_entry[i], xx = h.x_exit[i], yx = h.y_exit[i];
+    const float dx = xx - xe, dy = yx - ye;
+    const float len = sqrtf(dx * dx + dy * dy);
+    const float d = len > 0.0f ? fabsf(xe * yx - xx * ye) / len : 0.0f;
+    const float q = d * (1000.0f / (float)g.recon_cyl_radius);
+    key[i] = q < 1.0e6f ? 1u + (uint32_t)q : 1000000u;
+}
+
+__global__ void __launch_bounds__(128) k_endpoints_fast(DevGeom g, int64_t n, const uint32_t* __restrict__ order,
+                                                        const uint8_t* __restrict__ hull, HistView h,
+                                                        uint8_t* __restrict__ keep,
                                                         unsigned long long* __restrict__ flags) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (order) i = order[i];
     double xi = 0, yi = 0, zi = 0, xo = 0, yo = 0, zo = 0;
     int vx = 0, vy = 0, vz = 0, vx2 = 0, vy2 = 0, vz2 = 0;
     unsigned long long exact = 0;
@@ -792,59 +808,6 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     return s;
 }
 
-/* Launch order for k_mlp_fast: each chunk of MLP_ORDER_CHUNK histories counting-
- * sorted by sample count, so that the 32 histories of a warp run about the same
- * number of samples (the rows and their slots do not depend on the order). */
-constexpr int MLP_ORDER_CHUNK = 4096;
-constexpr int MLP_ORDER_KEYS = 1024;
-__global__ void __launch_bounds__(1024) k_mlp_order(int64_t n, const int64_t* __restrict__ bound,
-                                                    uint32_t* __restrict__ order) {
-    __shared__ int cnt[MLP_ORDER_KEYS];
-    __shared__ int wsum[32];
-    const int64_t base = (int64_t)blockIdx.x * MLP_ORDER_CHUNK;
-    const int m = (int)(n - base < MLP_ORDER_CHUNK ? n - base : MLP_ORDER_CHUNK);
-    for (int k = threadIdx.x; k < MLP_ORDER_KEYS; k += blockDim.x) cnt[k] = 0;
-    __syncthreads();
-    constexpr int PER = MLP_ORDER_CHUNK / 1024;
-    int key[PER], rank[PER];
-#pragma unroll
-    for (int r = 0; r < PER; ++r) {
-        const int t = threadIdx.x + r * 1024;
-        key[r] = -1;
-        if (t < m) {
-            const int64_t b = bound[base + t];
-            key[r] = (int)(b < MLP_ORDER_KEYS - 1 ? b : MLP_ORDER_KEYS - 1);
-            rank[r] = atomicAdd(&cnt[key[r]], 1);
-        }
-    }
-    __syncthreads();
-    /* exclusive scan of the 1024 bucket counts, one per thread */
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int v = cnt[threadIdx.x], incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) wsum[w] = incl;
-    __syncthreads();
-    if (w == 0) {
-        int s = wsum[lane], si = s;
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, si, o);
-            if (lane >= o) si += y;
-        }
-        wsum[lane] = si - s;
-    }
-    __syncthreads();
-    const int excl = incl - v + wsum[w];
-    __syncthreads();
-    cnt[threadIdx.x] = excl;
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < PER; ++r)
-        if (key[r] >= 0) order[base + cnt[key[r]] + rank[r]] = (uint32_t)(base + threadIdx.x + r * 1024);
-}
-
 /* Fills the row slot of each history.  A sample within `margin` of a voxel
  * face has two candidate voxels; when they are exactly the previous row entry
  * and the (certain) next sample's voxel, either choice gives the same row
@@ -1126,9 +1089,21 @@ pct_status pct_stage_endpoints(pct_ctx* c) {
         if (c->cfg.walk_exact)
             k_endpoints<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, c->x_hull_filtered.as<uint8_t>(), h,
                                                                      keep, c->err_flags.as<unsigned long long>());
-        else
-            k_endpoints_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
-                c->dg, n, c->x_hull_filtered.as<uint8_t>(), h, keep, c->err_flags.as<unsigned long long>());
+        else {
+            uint32_t* order = nullptr;
+            if (n <= (int64_t)0xffffffffu) {
+                PCT_TRY(c->walk_order.alloc(sizeof(uint32_t) * 2 * (size_t)n));
+                order = c->walk_order.as<uint32_t>();
+                uint32_t* key = order + n;
+                c->launches += 2;
+                k_endpoint_key<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, key);
+                k_chunk_order<uint32_t><<<(unsigned)((n + ORDER_CHUNK - 1) / ORDER_CHUNK), 1024, 0, c->stream>>>(
+                    n, key, order);
+            }
+            k_endpoints_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(c->dg, n, order,
+                                                                          c->x_hull_filtered.as<uint8_t>(), h, keep,
+                                                                          c->err_flags.as<unsigned long long>());
+        }
         PCT_CUDA(cudaGetLastError());
     }
     int64_t kept = 0;
@@ -1217,7 +1192,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
             PCT_TRY(c->mlp_order.alloc(sizeof(uint32_t) * n));
             order = c->mlp_order.as<uint32_t>();
             ++c->launches;
-            k_mlp_order<<<(unsigned)((n + MLP_ORDER_CHUNK - 1) / MLP_ORDER_CHUNK), 1024, 0, c->stream>>>(
+            k_chunk_order<int64_t><<<(unsigned)((n + ORDER_CHUNK - 1) / ORDER_CHUNK), 1024, 0, c->stream>>>(
                 n, c->mlp_bound.as<int64_t>(), order);
         }
         ++c->launches;

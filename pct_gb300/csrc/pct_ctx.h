@@ -138,6 +138,7 @@ struct pct_ctx {
     /* MLP rows and DROP */
     DevBuf row_offsets, row_len, rows, chord, row_scale, mlp_table;  /* row_offsets: start of each row's slot */
     DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows, mlp_order;  /* MLP row generation scratch */
+    DevBuf walk_order;                                               /* hull walk launch order + keys */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
     DevBuf block_norm;             /* per DROP block: sum of c^2 per voxel (robust variant) */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */

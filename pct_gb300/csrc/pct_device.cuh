@@ -128,6 +128,64 @@ __device__ __forceinline__ int cmp_le(float a, float ea, float b, float eb) {
     return -1;
 }
 
+/* Launch order for per-history kernels whose work per thread varies: each chunk
+ * of ORDER_CHUNK histories counting-sorted by an integer work estimate (clamped
+ * to ORDER_KEYS - 1), so that the 32 histories of a warp do about the same
+ * amount of work.  order[] is a permutation of [0, n) within each chunk; the
+ * results of the ordered kernels do not depend on it.  1024 threads per CTA. */
+constexpr int ORDER_CHUNK = 4096;
+constexpr int ORDER_KEYS = 1024;
+template <typename K>
+__global__ void __launch_bounds__(1024) k_chunk_order(int64_t n, const K* __restrict__ key,
+                                                      uint32_t* __restrict__ order) {
+    __shared__ int cnt[ORDER_KEYS];
+    __shared__ int wsum[32];
+    const int64_t base = (int64_t)blockIdx.x * ORDER_CHUNK;
+    const int m = (int)(n - base < ORDER_CHUNK ? n - base : ORDER_CHUNK);
+    for (int k = threadIdx.x; k < ORDER_KEYS; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    constexpr int PER = ORDER_CHUNK / 1024;
+    int kk[PER], rank[PER];
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+        const int t = threadIdx.x + r * 1024;
+        kk[r] = -1;
+        if (t < m) {
+            const K b = key[base + t];
+            kk[r] = b <= (K)0 ? 0 : (b < (K)(ORDER_KEYS - 1) ? (int)b : ORDER_KEYS - 1);
+            rank[r] = atomicAdd(&cnt[kk[r]], 1);
+        }
+    }
+    __syncthreads();
+    /* exclusive scan of the 1024 bucket counts, one per thread */
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int v = cnt[threadIdx.x];
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const int s = wsum[lane];
+        int si = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= o) si += y;
+        }
+        wsum[lane] = si - s;
+    }
+    __syncthreads();
+    const int excl = incl - v + wsum[w];
+    __syncthreads();
+    cnt[threadIdx.x] = excl;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < PER; ++r)
+        if (kk[r] >= 0) order[base + cnt[kk[r]] + rank[r]] = (uint32_t)(base + threadIdx.x + r * 1024);
+}
+
 static inline unsigned pct_grid_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     return (unsigned)(b > 0 ? b : 1);
