@@ -259,6 +259,7 @@ def main():
         for _ in range(a.steps):
             st = step()
             drop_s += st.seconds
+            form_ran = st.drop_form
         ev1.record(stream)
         torch.cuda.synchronize()
     if dist:
@@ -390,7 +391,8 @@ def main():
                                    " block %d, lambda %.2g" % (n, R, iters, cfg.block_size, cfg.lambda_),
                        "row_entries": rows, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "inputs larger than L2 (MLP rows %.1f GB)" % (rows * 4 / 1e9),
-                       "drop_form": forms[a.drop_form], "voxel_order": ["bricks", "linear"][a.voxel_order],
+                       "drop_form": forms[a.drop_form], "drop_form_ran": forms.get(form_ran, str(form_ran)),
+                       "voxel_order": ["bricks", "linear"][a.voxel_order],
                        "mlp_fp64_samples_per_step": (c1["mlp_fp64_samples"]),
                        "mlp_queue_capacity": max(R, 1 << 20),
                        "rows_ms_per_step": mlp_s / a.steps * 1e3, "drop_ms_per_iteration": drop_iter_s * 1e3},

@@ -193,6 +193,7 @@ typedef struct pct_drop_stats {
     int iterations_run;
     double residual[64];             /* FP64 relative data residual ||b - A x|| / ||b|| before each iteration, and after the last */
     double seconds;                  /* device time of the iterations */
+    int drop_form;                   /* the DROP form that ran (PCT_DROP_*: a form that does not fit falls back) */
 } pct_drop_stats;
 
 /* Arrays readable with pct_get_array().  H_* are per-history arrays of the

@@ -579,6 +579,7 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
         double b2 = res_host[maxit + 1];
         for (int k = 0; k < done && k < maxit; ++k) stats->residual[k] = b2 > 0 ? sqrt(res_host[k] / b2) : 0.0;
         stats->seconds = ms * 1e-3;
+        stats->drop_form = c->drop_mode;
     }
     return PCT_OK;
 }

@@ -7,10 +7,10 @@
  *   k_filter       filter_GPU (.cu:3036-3069): one CTA per (v, angle) sinogram
  *                  row, the row staged in shared memory, one thread per output
  *                  t bin accumulating in binary32 in the reference's order
- *   k_backproject  backprojection_GPU (.cu:3155-3230): one thread per voxel,
- *                  binary32 accumulation over angle bins in order, per-angle
- *                  cos/sin table in shared memory; the sinogram (NUM_BINS
- *                  floats) stays L2-resident
+ *   k_backproject  backprojection_GPU (.cu:3155-3230): one thread per voxel
+ *                  column and 16 slices, binary32 accumulation over angle bins
+ *                  in order per voxel, per-angle cos/sin table in shared
+ *                  memory; the sinogram (NUM_BINS floats) stays L2-resident
  *   k_fbp_hull     FBP_image_2_hull_GPU (.cu:3250)
  *   k_initial      define_initial_iterate (.cu:7191-7205)
  * Bound by binary64 throughput (each term of the reference is binary64).
@@ -70,54 +70,76 @@ __global__ void k_filter(int T, int A, double tb, const float* __restrict__ sino
     }
 }
 
-__global__ void k_backproject(DevGeom g, const float* __restrict__ sino, const double2* __restrict__ trig,
-                              float* __restrict__ image) {
+/* One thread per voxel column (x, y) and group of BP_SLICES slices: the terms
+ * of an angle that do not depend on z (u, t, the t bin, eta and the fan-beam
+ * scale, three binary64 divisions) are formed once per column and angle, the z
+ * terms (two divisions) per slice; each slice keeps its own binary32
+ * accumulator over the angle bins in order.  Every expression is the one of
+ * backprojection_GPU, so the image is the same bit for bit. */
+constexpr int BP_SLICES = 16;
+__global__ void __launch_bounds__(128) k_backproject(DevGeom g, const float* __restrict__ sino,
+                                                     const double2* __restrict__ trig, float* __restrict__ image) {
     extern __shared__ double2 strig[];
     for (int k = threadIdx.x; k < g.angular_bins; k += blockDim.x) strig[k] = trig[k];
     __syncthreads();
-    int voxel = blockIdx.x * blockDim.x + threadIdx.x;
-    if (voxel >= g.num_voxels) return;
-    int column = voxel % g.columns, row = (voxel / g.columns) % g.rows, slice = voxel / (g.columns * g.rows);
+    const int CR = g.columns * g.rows;
+    const int cr = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cr >= CR) return;
+    const int s_first = blockIdx.y * BP_SLICES;
+    const int ns = g.slices - s_first < BP_SLICES ? g.slices - s_first : BP_SLICES;
+    const int column = cr % g.columns, row = cr / g.columns;
     const double R = g.recon_cyl_radius, SR = g.source_radius;
     const double delta = g.gantry_angle_interval * PCT_ANGLE_TO_RADIANS;
     const int T = g.t_bins, ATB = g.angular_bins * g.t_bins, NB = g.num_bins;
-    double x = -R + (column + 0.5) * g.voxel_width;
-    double y = R - (row + 0.5) * g.voxel_height;
-    double z = -g.recon_cyl_height / 2.0 + (slice + 0.5) * g.slice_thickness;
+    const double x = -R + (column + 0.5) * g.voxel_width;
+    const double y = R - (row + 0.5) * g.voxel_height;
     if ((x * x + y * y) > (R * R)) {
-        image[voxel] = (float)PCT_RSP_AIR;
+        for (int k = 0; k < ns; ++k) image[(size_t)(s_first + k) * CR + cr] = (float)PCT_RSP_AIR;
         return;
     }
-    float acc = 0.0f;
+    double z[BP_SLICES];
+    float acc[BP_SLICES];
+#pragma unroll
+    for (int k = 0; k < BP_SLICES; ++k) {
+        z[k] = -g.recon_cyl_height / 2.0 + (s_first + k + 0.5) * g.slice_thickness;
+        acc[k] = 0.0f;
+    }
     for (int ab = 0; ab < g.angular_bins; ++ab) {
-        double ca = strig[ab].x, sa = strig[ab].y;
-        double u = x * ca + y * sa;
-        double t = -x * sa + y * ca;
-        double v = z;
-        double dnt = (t - u * (t / (SR + u))) / g.t_bin_size + T / 2.0;
+        const double ca = strig[ab].x, sa = strig[ab].y;
+        const double u = x * ca + y * sa;
+        const double t = -x * sa + y * ca;
+        const double dnt = (t - u * (t / (SR + u))) / g.t_bin_size + T / 2.0;
         int t_bin = pct_d2i(dnt);
         if (t_bin > dnt) t_bin -= 1;
-        double eta = dnt - t_bin;
-        double dnv = (v - u * (v / (SR + u))) / g.v_bin_size + g.v_bins / 2.0;
-        int v_bin = pct_d2i(dnv);
-        if (v_bin > dnv) v_bin -= 1;
-        double eps = dnv - v_bin;
-        double sf = SR / (SR + u);
-        double scale = sf * sf;
-        int bin = t_bin + ab * T + v_bin * ATB;
-        /* bins outside the sinogram read as 0 (the reference reads out of bounds there) */
-        float s0 = (bin >= 0 && bin < NB) ? sino[bin] : 0.0f;
-        float s1 = (bin + 1 >= 0 && bin + 1 < NB) ? sino[bin + 1] : 0.0f;
-        if (v_bin == g.v_bins - 1 || (bin < 0)) {
-            acc = (float)(acc + scale * (((1 - eta) * s0) + (eta * s1)));
-        } else {
-            float s2 = (bin + ATB >= 0 && bin + ATB < NB) ? sino[bin + ATB] : 0.0f;
-            float s3 = (bin + ATB + 1 >= 0 && bin + ATB + 1 < NB) ? sino[bin + ATB + 1] : 0.0f;
-            acc = (float)(acc + scale * ((1 - eta) * (1 - eps) * s0 + eta * (1 - eps) * s1 + (1 - eta) * eps * s2 +
-                                         eta * eps * s3));
+        const double eta = dnt - t_bin;
+        const double sf = SR / (SR + u);
+        const double scale = sf * sf;
+        const int tbin_ab = t_bin + ab * T;
+#pragma unroll
+        for (int k = 0; k < BP_SLICES; ++k) {
+            if (k >= ns) break;
+            const double v = z[k];
+            const double dnv = (v - u * (v / (SR + u))) / g.v_bin_size + g.v_bins / 2.0;
+            int v_bin = pct_d2i(dnv);
+            if (v_bin > dnv) v_bin -= 1;
+            const double eps = dnv - v_bin;
+            const int bin = tbin_ab + v_bin * ATB;
+            /* bins outside the sinogram read as 0 (the reference reads out of bounds there) */
+            const float s0 = (bin >= 0 && bin < NB) ? sino[bin] : 0.0f;
+            const float s1 = (bin + 1 >= 0 && bin + 1 < NB) ? sino[bin + 1] : 0.0f;
+            if (v_bin == g.v_bins - 1 || (bin < 0)) {
+                acc[k] = (float)(acc[k] + scale * (((1 - eta) * s0) + (eta * s1)));
+            } else {
+                const float s2 = (bin + ATB >= 0 && bin + ATB < NB) ? sino[bin + ATB] : 0.0f;
+                const float s3 = (bin + ATB + 1 >= 0 && bin + ATB + 1 < NB) ? sino[bin + ATB + 1] : 0.0f;
+                acc[k] = (float)(acc[k] + scale * ((1 - eta) * (1 - eps) * s0 + eta * (1 - eps) * s1 +
+                                                   (1 - eta) * eps * s2 + eta * eps * s3));
+            }
         }
     }
-    image[voxel] = (float)(acc * delta);
+#pragma unroll
+    for (int k = 0; k < BP_SLICES; ++k)
+        if (k < ns) image[(size_t)(s_first + k) * CR + cr] = (float)(acc[k] * delta);
 }
 
 __global__ void k_trig_bp(int n, double delta, double2* __restrict__ out) {
@@ -180,8 +202,10 @@ pct_status pct_stage_fbp(pct_ctx* c) {
     size_t bsm = sizeof(double2) * A;
     if (bsm > 48 * 1024) PCT_CUDA(cudaFuncSetAttribute(k_backproject, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
     ++c->launches;
-    k_backproject<<<pct_grid_for(V, 128), 128, bsm, c->stream>>>(c->dg, c->sinogram_filtered.as<float>(),
-                                                                 trig.as<double2>(), c->fbp_image.as<float>());
+    const dim3 bp_grid(pct_grid_for((int64_t)c->geo.columns * c->geo.rows, 128),
+                       (unsigned)((c->geo.slices + BP_SLICES - 1) / BP_SLICES));
+    k_backproject<<<bp_grid, 128, bsm, c->stream>>>(c->dg, c->sinogram_filtered.as<float>(), trig.as<double2>(),
+                                                    c->fbp_image.as<float>());
     ++c->launches;
     k_fbp_hull<<<pct_grid_for(V, 256), 256, 0, c->stream>>>(c->dg, c->cfg.fbp_threshold, c->fbp_image.as<float>(),
                                                             c->fbp_hull.as<uint8_t>());

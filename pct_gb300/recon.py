@@ -34,7 +34,8 @@ class Counts(C.Structure):
 
 
 class DropStats(C.Structure):
-    _fields_ = [("iterations_run", C.c_int), ("residual", C.c_double * 64), ("seconds", C.c_double)]
+    _fields_ = [("iterations_run", C.c_int), ("residual", C.c_double * 64), ("seconds", C.c_double),
+                ("drop_form", C.c_int)]
 
 
 ARRAYS = ["MSC_COUNTS", "SM_COUNTS", "SC_HULL", "MSC_HULL", "SM_HULL", "BIN_COUNTS_PRE", "MEAN_WEPL", "MEAN_UT",

@@ -178,7 +178,8 @@ def test_drop_within_tolerance_of_fp64(run):
 @pytest.mark.parametrize("form", [1, 2])
 def test_drop_other_forms_within_tolerance(run, form):
     """The sorted (1) and tiled (2) forms of the DROP block step against the
-    same binary64 iterate (the default scatter form is checked above)."""
+    same binary64 iterate (the default scatter form is checked above); the form
+    asked for is the one that ran."""
     name, cfg, ora, out = run
     its = cfg.iterations
     if its == 0:
@@ -192,9 +193,10 @@ def test_drop_other_forms_within_tolerance(run, form):
     r = recon.run_full(cfg2, data, angles)
     r.collect_mlp_endpoints()
     r.mlp_rows()
-    r.drop(its)
+    st = r.drop(its)
     x = r.array("X").astype(np.float64)
     r.close()
+    assert st.drop_form == form
     ref = ora["x_%d" % its]
     err = np.linalg.norm(x - ref) / np.linalg.norm(ref)
     assert err <= DROP_TOL, "relative L2 %.3e" % err
@@ -228,8 +230,9 @@ def test_drop_tiled_form_is_reproducible(run):
     assert same(images[0], images[2])
 
 
+@pytest.mark.parametrize("form", [0, 1])
 @pytest.mark.parametrize("variant", [1, 2])
-def test_drop_variants_within_tolerance(run, variant):
+def test_drop_variants_within_tolerance(run, variant, form):
     """DROP_blocks_red (1) and DROP_blocks_robust2 + DROP_update_robust2 (2) on
     the GPU against the oracle's binary64 run of the same iterations.  eta is
     kept small: with the reference default 2.5, psi = (1 - x) eta is negative
@@ -243,6 +246,7 @@ def test_drop_variants_within_tolerance(run, variant):
     for f, _ in cfg._fields_:
         setattr(cfg2, f, getattr(cfg, f))
     cfg2.drop_variant = variant
+    cfg2.drop_form = form
     eta = 0.05 if variant == 1 else 0.005  # psi well below ||a||^2, and below ||A|| of a voxel crossed once
     cfg2.eta = eta
     cfg2.psi_sign = 1
@@ -251,9 +255,10 @@ def test_drop_variants_within_tolerance(run, variant):
     r = recon.run_full(cfg2, data, angles)
     r.collect_mlp_endpoints()
     r.mlp_rows()
-    r.drop(its)
+    st = r.drop(its)
     x = r.array("X").astype(np.float64)
     r.close()
+    assert st.drop_form == form
     offs, rows, chord = oracle.mlp_rows(cfg, ora["_hr"])
     ref = oracle.drop_variant(cfg, offs, rows, chord, ora["_hr"]["WEPL"], ora["x_k0"], its, cfg.block_size,
                               float(np.float32(cfg.lambda_)), variant, eta, 1)
