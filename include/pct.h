@@ -108,6 +108,9 @@ typedef struct pct_config {
                                       PCT_DROP_ROBUST2 (DROP_blocks_robust2 / DROP_update_robust2 .cu:7871-7901) */
     double eta;                    /* ETA (2.5) */
     int psi_sign;                  /* PSI_SIGN (1) */
+    int mlp_tabulated;             /* 1: MLP rows from the reference's lookup tables
+                                      (find_MLP_path_GPU_tabulated .cu:5502-5660, tables .cu:4786-4910),
+                                      binary64; 0: the analytic MLP (default) */
 } pct_config;
 
 enum { PCT_DROP_STANDARD = 0, PCT_DROP_RED = 1, PCT_DROP_ROBUST2 = 2 };

@@ -37,6 +37,7 @@ def load():
         path = build_oracle.build()
         _lib = C.CDLL(path)
         _lib.ora_mlp_rows.restype = C.c_int64
+        _lib.ora_mlp_rows_tab.restype = C.c_int64
         _lib.ora_effective_chord_length.restype = C.c_double
         _lib.ora_effective_chord_length.argtypes = [C.c_void_p, C.c_double, C.c_double]
         _lib.ora_drop.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -170,8 +171,9 @@ def endpoints(cfg, hull, h):
     return out
 
 
-def mlp_rows(cfg, h, capacity=None, threads=None):
-    """h: recon vectors (x_entry.. are the hull entry/exit points). Returns (offsets, rows, chord)."""
+def mlp_rows(cfg, h, capacity=None, threads=None, tabulated=False):
+    """h: recon vectors (x_entry.. are the hull entry/exit points). Returns (offsets, rows, chord).
+    tabulated: the reference's lookup-table MLP (ora_mlp_rows_tab)."""
     n = len(h["x_entry"])
     g = geometry(cfg)
     if capacity is None:
@@ -181,7 +183,10 @@ def mlp_rows(cfg, h, capacity=None, threads=None):
     chord = np.empty(n, np.float64)
     args = [_p(h[f]) for f in ("x_entry", "y_entry", "z_entry", "x_exit", "y_exit", "z_exit", "xy_entry_angle",
                                "xz_entry_angle", "xy_exit_angle", "xz_exit_angle")]
-    if threads:
+    if tabulated:
+        k = load().ora_mlp_rows_tab(_cfgp(cfg), C.c_int64(n), *args, _p(h["first_voxel"]), _p(offsets), _p(rows),
+                                    C.c_int64(capacity), _p(chord))
+    elif threads:
         k = load().ora_mlp_rows_mt(_cfgp(cfg), C.c_int64(n), *args, _p(h["first_voxel"]), _p(offsets), _p(rows),
                                    C.c_int64(capacity), _p(chord), C.c_int(threads))
     else:

@@ -955,6 +955,156 @@ int64_t ora_mlp_rows(const pct_config* cfg, int64_t n, const float* x_in, const 
     return pos;
 }
 
+/* Tabulated MLP (.cu:5502-5660).  Tables (.cu:4786-4911): sin/cos of
+ * -2 pi + i * 0.001 deg for i <= (6 pi) / step + 0.5; per depth du = k * 5e-5 cm
+ * (k <= 800000) the five moment polynomials and the scattering coefficient
+ * pow(E_0 (1 + 0.038 log(du / X0)), 2) / X0. */
+#define ORA_TRIG_MIN (-2 * PCT_PI)
+#define ORA_TRIG_STEP (0.001 * PCT_ANGLE_TO_RADIANS)
+#define ORA_TRIG_N ((int)((4 * PCT_PI - -2 * PCT_PI) / ORA_TRIG_STEP + 0.5))
+#define ORA_DEPTH_STEP 0.00005
+#define ORA_DEPTH_N ((int)(40.0 / ORA_DEPTH_STEP + 0.5))
+
+static double* ora_tab_sin = NULL;
+static double* ora_tab_cos = NULL;
+static double* ora_tab_p12 = NULL;
+static double* ora_tab_p23 = NULL;
+static double* ora_tab_p34 = NULL;
+static double* ora_tab_p26 = NULL;
+static double* ora_tab_p312 = NULL;
+static double* ora_tab_sc = NULL;
+
+static int ora_tables(void) {
+    if (ora_tab_sin) return 0;
+    double* t[8];
+    const int64_t sz[8] = {ORA_TRIG_N + 1, ORA_TRIG_N + 1, ORA_DEPTH_N + 1, ORA_DEPTH_N + 1,
+                           ORA_DEPTH_N + 1, ORA_DEPTH_N + 1, ORA_DEPTH_N + 1, ORA_DEPTH_N + 1};
+    for (int k = 0; k < 8; ++k) {
+        t[k] = (double*)malloc(sizeof(double) * (size_t)sz[k]);
+        if (!t[k]) {
+            for (int j = 0; j < k; ++j) free(t[j]);
+            return 2;
+        }
+    }
+    for (int i = 0; i <= ORA_TRIG_N; ++i) {
+        double val = ORA_TRIG_MIN + i * ORA_TRIG_STEP;
+        t[0][i] = pct_sin(val);
+        t[1][i] = pct_cos(val);
+    }
+    for (int k = 0; k <= ORA_DEPTH_N; ++k) {
+        double du = k * ORA_DEPTH_STEP;
+        t[2][k] = du * (A0 + du * (AL(1, 2) + du * (AL(2, 3) + du * (AL(3, 4) + du * (AL(4, 5) + AU(du, 5, 6))))));
+        t[3][k] = (du * du) * (AL(0, 2) + du * (AL(1, 3) + du * (AL(2, 4) + du * (AL(3, 5) + du * (AL(4, 6) + AU(du, 5, 7))))));
+        t[4][k] = pct_cube(du) * (AL(0, 3) + du * (AL(1, 4) + du * (AL(2, 5) + du * (AL(3, 6) + du * (AL(4, 7) + AU(du, 5, 8))))));
+        t[5][k] = (du * du) * (AL(0, 2) + du * (AL(1, 6) + du * (AL(2, 12) + du * (AL(3, 20) + du * (AL(4, 30) + AU(du, 5, 42))))));
+        t[6][k] = pct_cube(du) * (AL(0, 3) + du * (AL(1, 12) + du * (AL(2, 30) + du * (AL(3, 60) + du * (AL(4, 105) + AU(du, 5, 168))))));
+        double e = PCT_E_0 * (1 + 0.038 * pct_log(du / PCT_X_0));
+        t[7][k] = k > 0 ? (e * e) / PCT_X_0 : 0.0;
+    }
+    ora_tab_sin = t[0]; ora_tab_cos = t[1]; ora_tab_p12 = t[2]; ora_tab_p23 = t[3];
+    ora_tab_p34 = t[4]; ora_tab_p26 = t[5]; ora_tab_p312 = t[6]; ora_tab_sc = t[7];
+    return 0;
+}
+
+static int64_t mlp_path_tab(const pct_geometry* g, double x_in, double y_in, double z_in, double x_out, double y_out,
+                            double z_out, double xy_entry, double xz_entry, double xy_exit, double xz_exit,
+                            uint32_t first_voxel, uint32_t* path, int64_t capacity) {
+    const double STEP = g->mlp_u_step;
+    int64_t n = 0;
+    if (capacity < 1) return -1;
+    path[n++] = first_voxel;
+    unsigned idx = (unsigned)((xy_entry - ORA_TRIG_MIN) / ORA_TRIG_STEP + 0.5);
+    if (idx > (unsigned)ORA_TRIG_N) return n;
+    double s = ora_tab_sin[idx], c = ora_tab_cos[idx];
+    double u_in = c * x_in + s * y_in;
+    double u_out = c * x_out + s * y_out;
+    if (u_in > u_out) {
+        xy_entry += PCT_PI;
+        xy_exit += PCT_PI;
+        idx = (unsigned)((xy_entry - ORA_TRIG_MIN) / ORA_TRIG_STEP + 0.5);
+        if (idx > (unsigned)ORA_TRIG_N) return n;
+        s = ora_tab_sin[idx];
+        c = ora_tab_cos[idx];
+        u_in = c * x_in + s * y_in;
+        u_out = c * x_out + s * y_out;
+    }
+    double t_in = c * y_in - s * x_in;
+    double t_out = c * y_out - s * x_out;
+    double T2b = xy_exit - xy_entry, V2b = xz_exit - xz_entry;
+    double u_2 = fabs(u_out - u_in);
+    double depth = u_2 - STEP;
+    double u_sh = u_in;
+    unsigned istep = (unsigned)(STEP / ORA_DEPTH_STEP + 0.5);
+    unsigned i1 = istep, i2 = (unsigned)(depth / ORA_DEPTH_STEP + 0.5), ip = istep;
+    unsigned iu2 = (unsigned)(u_2 / ORA_DEPTH_STEP + 0.5);
+    if (!(u_2 < 40.0) || iu2 > (unsigned)ORA_DEPTH_N) return n;
+    double q312 = ora_tab_p312[iu2], q26 = ora_tab_p26[iu2], q12 = ora_tab_p12[iu2];
+    uint32_t last = first_voxel;
+    while (depth > STEP) {
+        double a12 = ora_tab_p12[ip], a23 = ora_tab_p23[ip];
+        double st1 = ora_tab_p312[ip], stt1 = ora_tab_p26[ip], sth1 = a12;
+        double st2 = q312 - (u_2 * u_2) * a12 + 2 * u_2 * a23 - ora_tab_p34[ip];
+        double stt2 = q26 - u_2 * a12 + a23;
+        double sth2 = q12 - a12;
+        double d1 = ora_tab_sc[i1] * (st1 * sth1 - stt1 * stt1);
+        double A1 = sth1 / d1, B1 = stt1 / d1, C1 = st1 / d1;
+        double d2 = ora_tab_sc[i2] * (st2 * sth2 - stt2 * stt2);
+        double A2 = sth2 / d2, B2 = stt2 / d2, C2 = st2 / d2;
+        double common = A2 * depth - B2;
+        double f0 = A1 + A2;
+        double f1 = common - B1;
+        double f2 = depth * A2 - B1 - B2;
+        double f3 = C1 + C2 + depth * (common - B2);
+        double det = f0 * f3 - f1 * f2;
+        double k3 = A2 * t_out - B2 * T2b;
+        double e0 = A1 * t_in + k3;
+        double e1 = depth * k3 + C2 * T2b - B2 * t_out - B1 * t_in;
+        double t_1 = (f3 * e0 - f1 * e1) / det;
+        k3 = A2 * z_out - B2 * V2b;
+        e0 = A1 * z_in + k3;
+        e1 = depth * k3 + C2 * V2b - B2 * z_out - B1 * z_in;
+        double v_1 = (f3 * e0 - f1 * e1) / det;
+        u_sh += STEP;
+        double x_1 = c * u_sh - s * t_1;
+        double y_1 = s * u_sh + c * t_1;
+        int vx = calculate_voxel(g->x_zero, x_1, g->voxel_width);
+        int vy = calculate_voxel(g->y_zero, y_1, g->voxel_height);
+        int vz = calculate_voxel(g->z_zero, v_1, g->voxel_thickness);
+        uint32_t voxel = (uint32_t)(vx + vy * g->columns + vz * g->columns * g->rows);
+        if (voxel != last) {
+            if (n >= capacity) return -1;
+            path[n++] = voxel;
+            last = voxel;
+        }
+        depth -= STEP;
+        i1 += istep;
+        i2 -= istep;
+        ip += istep;
+    }
+    return n;
+}
+
+int64_t ora_mlp_rows_tab(const pct_config* cfg, int64_t n, const float* x_in, const float* y_in, const float* z_in,
+                         const float* x_out, const float* y_out, const float* z_out, const float* xy_entry_angle,
+                         const float* xz_entry_angle, const float* xy_exit_angle, const float* xz_exit_angle,
+                         const uint32_t* first_voxel, int64_t* offsets, uint32_t* rows, int64_t capacity,
+                         double* chord) {
+    pct_geometry g;
+    if (pct_geometry_derive(cfg, &g) || ora_tables()) return -1;
+    int64_t pos = 0;
+    offsets[0] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double ae = xy_entry_angle[i], ax = xy_exit_angle[i], ze = xz_entry_angle[i], zx = xz_exit_angle[i];
+        chord[i] = ora_effective_chord_length(cfg, (ae + ax) / 2.0, (ze + zx) / 2.0);
+        int64_t k = mlp_path_tab(&g, x_in[i], y_in[i], z_in[i], x_out[i], y_out[i], z_out[i], ae, ze, ax, zx,
+                                 first_voxel[i], rows + pos, capacity - pos);
+        if (k < 0) return -1;
+        pos += k;
+        offsets[i + 1] = pos;
+    }
+    return pos;
+}
+
 /* ------------------------------------------------------------------------- */
 /* a16-a19: DROP                                                              */
 /* ------------------------------------------------------------------------- */

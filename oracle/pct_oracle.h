@@ -85,6 +85,15 @@ int64_t ora_mlp_rows(const pct_config* cfg, int64_t n, const float* x_in, const 
                      const uint32_t* first_voxel, int64_t* offsets, uint32_t* rows, int64_t capacity, double* chord);
 double ora_effective_chord_length(const pct_config* cfg, double abs_angle_t, double abs_angle_v);
 
+/* a14 tabulated: find_MLP_path_GPU_tabulated (.cu:5502-5660) with the tables
+ * of .cu:4786-4911 at the resolutions of pCT_data.h:405-417; same outputs as
+ * ora_mlp_rows. */
+int64_t ora_mlp_rows_tab(const pct_config* cfg, int64_t n, const float* x_in, const float* y_in, const float* z_in,
+                         const float* x_out, const float* y_out, const float* z_out, const float* xy_entry_angle,
+                         const float* xz_entry_angle, const float* xy_exit_angle, const float* xz_exit_angle,
+                         const uint32_t* first_voxel, int64_t* offsets, uint32_t* rows, int64_t capacity,
+                         double* chord);
+
 /* a16-a19: DROP on precomputed rows, FP64 image; iterations over all blocks. */
 int ora_drop(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows, const double* chord,
              const float* wepl, int iterations, int block_size, double lambda, double* x);

@@ -40,6 +40,7 @@ class Config(C.Structure):
         ("residual_tol", C.c_double), ("chord_bf16", C.c_int), ("mlp_exact", C.c_int),
         ("mlp_face_margin", C.c_double), ("drop_form", C.c_int), ("walk_exact", C.c_int),
         ("voxel_order", C.c_int), ("drop_variant", C.c_int), ("eta", C.c_double), ("psi_sign", C.c_int),
+        ("mlp_tabulated", C.c_int),
     ]
 
 

@@ -1160,6 +1160,7 @@ static pct_status ensure_mlp_table(pct_ctx* c, int* kmax) {
 
 pct_status pct_stage_mlp_rows(pct_ctx* c) {
     if (c->stage < ST_ENDPOINTS) return pct_fail(PCT_ERR_STATE, "mlp_rows needs collect_mlp_endpoints");
+    if (c->cfg.mlp_tabulated) return pct_stage_mlp_rows_tab(c);
     const int64_t n = c->h.n;
     PCT_TRY(c->row_offsets.alloc(sizeof(int64_t) * (n + 1)));
     PCT_TRY(c->row_len.alloc(sizeof(int) * (n > 0 ? n : 1)));

@@ -262,6 +262,8 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     if (cfg->drop_form < PCT_DROP_SCATTER || cfg->drop_form > PCT_DROP_TILED)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_form %d", cfg->drop_form);
     if (cfg->mlp_hull < 0 || cfg->mlp_hull > 3) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: bad mlp_hull");
+    if (cfg->mlp_tabulated != 0 && cfg->mlp_tabulated != 1)
+        return pct_fail(PCT_ERR_ARGUMENT, "pct_create: mlp_tabulated %d", cfg->mlp_tabulated);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -300,7 +302,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->sc_hull, &c->msc_counts, &c->sm_counts, &c->msc_hull, &c->sm_hull, &c->fbp_image,
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
                      &c->rows, &c->chord, &c->row_scale, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
-                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order, &c->walk_order,
+                     &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order, &c->walk_order, &c->mlp_tab_trig, &c->mlp_tab_depth,
                      &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm};
     for (DevBuf* b : all) b->release();
     c->td.release();

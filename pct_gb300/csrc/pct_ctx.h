@@ -139,6 +139,7 @@ struct pct_ctx {
     DevBuf row_offsets, row_len, rows, chord, row_scale, mlp_table;  /* row_offsets: start of each row's slot */
     DevBuf mlp_bound, mlp_rec, mlp_queue, mlp_fix_rows, mlp_order;  /* MLP row generation scratch */
     DevBuf walk_order;                                               /* hull walk launch order + keys */
+    DevBuf mlp_tab_trig, mlp_tab_depth;                              /* tables of the tabulated MLP */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
     DevBuf block_norm;             /* per DROP block: sum of c^2 per voxel (robust variant) */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
@@ -176,6 +177,7 @@ pct_status pct_stage_hull_selection(pct_ctx* c);
 pct_status pct_stage_initial_iterate(pct_ctx* c);
 pct_status pct_stage_endpoints(pct_ctx* c);
 pct_status pct_stage_mlp_rows(pct_ctx* c);
+pct_status pct_stage_mlp_rows_tab(pct_ctx* c);
 pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats);
 
 /* Stable compaction of src[src_off, src_off+n) by a keep flag into dst at dst_off. */

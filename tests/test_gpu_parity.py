@@ -304,3 +304,25 @@ def test_bf16_chords_error_stated(run):
           % (name, err_bf, err))
     assert err_bf <= DROP_TOL
     assert err <= 2.0 ** -8
+
+
+def test_tabulated_mlp_rows_bit_exact(run):
+    """The tabulated MLP (mlp_tabulated = 1, find_MLP_path_GPU_tabulated) against
+    the oracle's restatement of it: the same rows bit for bit; the chords are the
+    analytic ones in both."""
+    name, cfg, ora, out = run
+    cfg2 = phantoms.make_config({})
+    for f, _ in cfg._fields_:
+        setattr(cfg2, f, getattr(cfg, f))
+    cfg2.mlp_tabulated = 1
+    w, _ = CASES[name]()
+    data, angles = phantoms.generate(w)
+    r = recon.run_full(cfg2, data, angles)
+    r.collect_mlp_endpoints()
+    r.mlp_rows()
+    offs_g, rows_g, chord_g = r.array("ROW_OFFSETS"), r.array("ROWS"), r.array("CHORD")
+    r.close()
+    offs, rows, chord = oracle.mlp_rows(cfg, ora["_hr"], tabulated=True)
+    assert same(offs_g, offs), mismatch(offs_g, offs)
+    assert same(rows_g, rows), mismatch(rows_g, rows)
+    assert same(chord_g, chord.astype(np.float32))
