@@ -41,7 +41,7 @@ __global__ void k_block_counts(int64_t start, int64_t end, const int64_t* __rest
     if (i >= end) return;
     int64_t a = row_start[i], b = a + row_len[i];
     for (int64_t p = a + lane; p < b; p += 32) {
-        uint32_t v = rows[p];
+        uint32_t v = __ldcs(rows + p); /* streamed once: evict first */
         if (v < nv) atomicAdd(cnt + v, 1u);
     }
 }
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
 #pragma unroll
         for (int k = 0; k < DROP_REG; ++k) {
             const int q = lane + 32 * k;
-            e[k] = q < len ? rows[a + q] : 0xffffffffu;
+            e[k] = q < len ? __ldcs(rows + a + q) : 0xffffffffu; /* streamed once: evict first */
         }
 #pragma unroll
         for (int k = 0; k < DROP_REG; ++k) xv[k] = e[k] < nv ? x[e[k]] : 0.0f;
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
 #pragma unroll
         for (int k = 0; k < DROP_REG; ++k) dot += xv[k];
         for (int q = 32 * DROP_REG + lane; q < len; q += 32) {
-            const uint32_t v = rows[a + q];
+            const uint32_t v = __ldcs(rows + a + q);
             if (v < nv) dot += x[v];
         }
         for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
             for (int k = 0; k < DROP_REG; ++k)
                 if (e[k] < nv) atomicAdd(upd + e[k], cl_res / (aa + ((1.0f - xv[k]) * eta) * psi_sign));
             for (int q = 32 * DROP_REG + lane; q < len; q += 32) {
-                const uint32_t v = rows[a + q];
+                const uint32_t v = __ldcs(rows + a + q);
                 if (v < nv) atomicAdd(upd + v, cl_res / (aa + ((1.0f - x[v]) * eta) * psi_sign));
             }
         } else {
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
             for (int k = 0; k < DROP_REG; ++k)
                 if (e[k] < nv) atomicAdd(upd + e[k], value);
             for (int q = 32 * DROP_REG + lane; q < len; q += 32) {
-                const uint32_t v = rows[a + q];
+                const uint32_t v = __ldcs(rows + a + q);
                 if (v < nv) atomicAdd(upd + v, value);
             }
         }
