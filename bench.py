@@ -46,7 +46,12 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--histories", type=int, default=30_000_000)
+    ap.add_argument("--histories", type=int, default=None,
+                    help="scan size (default: 30M for cfg2, 60M for cfg4)")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg4"],
+                    help="cfg2 (the bench line: 256x256x32, 8-insert cylinder) or cfg4 (320x320x64 head phantom)")
+    ap.add_argument("--chord-bf16", type=int, default=None, choices=[0, 1],
+                    help="round chords to bfloat16 (default: the workload's setting; cfg4 uses bf16)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=6000)
@@ -55,7 +60,10 @@ def parse():
                     help="DROP block step: 0 scatter (default), 1 sorted, 2 tiled")
     ap.add_argument("--voxel-order", type=int, default=0, choices=[0, 1],
                     help="internal voxel order: 0 bricks where the grid allows (default), 1 linear")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.histories is None:
+        a.histories = 60_000_000 if a.workload == "cfg4" else 30_000_000
+    return a
 
 
 def dist_env():
@@ -218,8 +226,11 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    w = phantoms.cfg2(num_histories=a.histories, seed=2 + rank)
+    make_workload = phantoms.cfg4 if a.workload == "cfg4" else phantoms.cfg2
+    w = make_workload(num_histories=a.histories, seed=(4 if a.workload == "cfg4" else 2) + rank)
     over = dict(w.config)
+    if a.chord_bf16 is not None:
+        over["chord_bf16"] = a.chord_bf16
     over["drop_form"] = a.drop_form
     over["voxel_order"] = a.voxel_order
     cfg = phantoms.make_config(over)
@@ -387,8 +398,10 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": t / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded phantom generator, PCTD layout)",
-            "config": {"workload": "cfg2: %d histories, %d recon histories, 180 angles, 256x256x32, %d DROP iterations,"
-                                   " block %d, lambda %.2g" % (n, R, iters, cfg.block_size, cfg.lambda_),
+            "config": {"workload": "%s: %d histories, %d recon histories, %d angles, %dx%dx%d, %d DROP iterations,"
+                                   " block %d, lambda %.2g, %s chords"
+                                   % (a.workload, n, R, w.num_angles, g.columns, g.rows, g.slices, iters,
+                                      cfg.block_size, cfg.lambda_, "bf16" if cfg.chord_bf16 else "binary32"),
                        "row_entries": rows, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "inputs larger than L2 (MLP rows %.1f GB)" % (rows * 4 / 1e9),
                        "drop_form": forms[a.drop_form], "drop_form_ran": forms.get(form_ran, str(form_ran)),
