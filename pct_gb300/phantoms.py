@@ -114,11 +114,14 @@ def cfg4(num_histories=60_000_000, seed=4):
         t_extent=12.2, v_extent=8.05, seed=seed)
 
 
-def ellipsoids(seed, num_histories=None):
-    """Random ellipsoid phantom of the batched-scan workload (3-12 ellipsoids, RSP 0.2-1.9)."""
+def ellipsoids(seed, num_histories=None, cols=None, slices=None):
+    """Random ellipsoid phantom of the batched-scan workload (3-12 ellipsoids, RSP 0.2-1.9);
+    the grid (128-256 columns, 8-48 slices) is drawn from the seed unless given."""
     rng = random.Random(seed)
-    cols = rng.choice([128, 160, 192, 224, 256])
-    slices = rng.choice([8, 16, 24, 32, 40, 48])
+    cols_drawn = rng.choice([128, 160, 192, 224, 256])
+    slices_drawn = rng.choice([8, 16, 24, 32, 40, 48])
+    cols = cols_drawn if cols is None else cols
+    slices = slices_drawn if slices is None else slices
     r_cyl = cols * 0.1 / 2
     body_a = r_cyl * rng.uniform(0.55, 0.75)
     body_b = r_cyl * rng.uniform(0.55, 0.75)
