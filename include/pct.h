@@ -343,6 +343,10 @@ enum { PCT_DT_F32 = 0, PCT_DT_U32 = 1, PCT_DT_F64 = 2 };
 typedef int (*pct_allreduce_fn)(void* user, void* data, int64_t count, int dtype, int on_device);
 pct_status pct_set_allreduce(pct_ctx* ctx, pct_allreduce_fn fn, void* user);
 pct_status pct_select_shard(pct_ctx* ctx, int shard, int num_shards);
+/* DROP block size (BLOCK_SIZE_RECON) of an existing context, e.g. for a
+ * block-size search; takes effect at the next pct_drop (the diagonal weights
+ * are recounted).  Not for a context that holds a shard. */
+pct_status pct_set_block_size(pct_ctx* ctx, int block_size);
 /* cudaMemcpy with the direction taken from the pointers (for callbacks). */
 pct_status pct_memcpy(void* dst, const void* src, int64_t bytes);
 

@@ -521,6 +521,18 @@ extern "C" pct_status pct_select_shard(pct_ctx* c, int shard, int num_shards) {
     return PCT_OK;
 }
 
+extern "C" pct_status pct_set_block_size(pct_ctx* c, int block_size) {
+    if (!c) return pct_fail(PCT_ERR_ARGUMENT, "null context");
+    if (block_size < 1) return pct_fail(PCT_ERR_ARGUMENT, "pct_set_block_size: %d", block_size);
+    if (c->num_shards != 1) return pct_fail(PCT_ERR_STATE, "pct_set_block_size: the context holds a shard");
+    if (block_size != c->cfg.block_size) {
+        c->cfg.block_size = block_size;
+        c->diag_ready = 0;
+        pct_drop_release_graph(c);
+    }
+    return PCT_OK;
+}
+
 extern "C" pct_status pct_memcpy(void* dst, const void* src, int64_t bytes) {
     if (bytes < 0 || (bytes > 0 && (!dst || !src))) return pct_fail(PCT_ERR_ARGUMENT, "pct_memcpy: bad arguments");
     if (bytes == 0) return PCT_OK;

@@ -77,6 +77,7 @@ def _declare(lib):
     lib.pct_select_shard.argtypes = [vp, ci, ci]
     lib.pct_set_allreduce.argtypes = [vp, _capi.ALLREDUCE_FN, vp]
     lib.pct_memcpy.argtypes = [vp, vp, i64]
+    lib.pct_set_block_size.argtypes = [vp, ci]
 
 
 class Reconstruction:
@@ -185,6 +186,11 @@ class Reconstruction:
     def reset_iterate(self):
         self._call("pct_reset_iterate")
 
+    def set_block_size(self, block_size):
+        """DROP block size for the next drop() (pct_set_block_size)."""
+        self._call("pct_set_block_size", int(block_size))
+        self.cfg.block_size = int(block_size)
+
     def select_shard(self, shard, num_shards):
         """Keeps this rank's share of every DROP block (pct_select_shard)."""
         self._call("pct_select_shard", int(shard), int(num_shards))
@@ -224,9 +230,9 @@ class Reconstruction:
         return self.lib.pct_stream(self.h)
 
 
-def run_full(config, data13, projection_angle, chunk=None):
+def run_full(config, data13, projection_angle, chunk=None, device=0):
     """The whole reference sequence on one host dataset; returns the context."""
-    r = Reconstruction(config)
+    r = Reconstruction(config, device=device)
     n = data13.shape[1]
     r.reserve(n)
     chunk = chunk or n
