@@ -12,6 +12,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libpct_gb300.so")
 
 PCT_OK = 0
+(PCT_ERR_ARGUMENT, PCT_ERR_CUDA, PCT_ERR_ALLOC, PCT_ERR_STATE, PCT_ERR_OVERFLOW, PCT_ERR_TIMEOUT, PCT_ERR_IO,
+ PCT_ERR_NUMERIC) = range(1, 9)
 
 
 class PctError(RuntimeError):
