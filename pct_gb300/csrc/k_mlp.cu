@@ -14,8 +14,11 @@
  *                 depth u_2, so each row gets a slot of that size (k_mlp_bound +
  *                 scan) and one pass fills it; binary32 samples with a binary64
  *                 recomputation near voxel faces (see below).
- *   k_row_norms   EffectiveChordLength_GPU (.cu:4974-4995) per row and the DROP
- *                 row norm ||a_i||^2 = c^2 n (.cu:5825) kept as 1/||a_i||^2 in binary64.
+ *   chords        EffectiveChordLength_GPU (.cu:4974-4995) per row, in binary64
+ *                 inside k_mlp_fast (its FP64 work overlaps the binary32 samples),
+ *                 and the DROP row scale 1 / (c n) from ||a_i||^2 = c^2 n (.cu:5825)
+ *                 once the row length is final (k_mlp_fast or k_mlp_dedupe);
+ *                 k_row_norms does both for rows read from a file.
  */
 #include <cuda_bf16.h>
 #include "pct_device.cuh"
@@ -808,6 +811,34 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     return s;
 }
 
+/* EffectiveChordLength_GPU (.cu:4974-4995) with correctly rounded sinf/cosf */
+__device__ double dev_chord(const DevGeom& g, double abs_angle_t, double abs_angle_v) {
+    const double VW = g.voxel_width, VT = g.voxel_thickness, STEP = g.mlp_u_step;
+    double eff_t = abs_angle_t - ((int)(abs_angle_t / (PCT_PI / 2))) * (PCT_PI / 2);
+    double eff_v = fabs(abs_angle_v);
+    double sf = STEP / VW;
+    float s2t = pct_sinf((float)(2 * eff_t)), ct = pct_cosf((float)eff_t), st = pct_sinf((float)eff_t);
+    double c2d = (1 / 3.0) * ((sf * sf * s2t - 6) / (sf * s2t - 2 * (ct + st)) + sf * sf * s2t / (2 * (ct + st)));
+    double mean_pixel_width = VW / (ct + st);
+    double hf = VT / mean_pixel_width;
+    sf = STEP / mean_pixel_width;
+    float s2v = pct_sinf((float)(2 * eff_v)), cv = pct_cosf((float)eff_v), sv = pct_sinf((float)eff_v);
+    double c3d = (1 / 3.0) * ((sf * sf * s2v - 6 * hf) / (sf * s2v - 2 * (hf * cv + sv)) + sf * sf * s2v / (2 * (hf * cv + sv)));
+    return VW * c2d * c3d;
+}
+
+/* The row's chord length (bf16: rounded to bfloat16, nearest even); out of
+ * line so that its binary64 code stays out of the callers' register budget. */
+__device__ __noinline__ float dev_row_chord(const DevGeom& g, const HistView& h, int64_t i, int bf16) {
+    const double ae = h.xy_entry_angle[i], ax = h.xy_exit_angle[i], ze = h.xz_entry_angle[i], zx = h.xz_exit_angle[i];
+    double c = dev_chord(g, (ae + ax) / 2.0, (ze + zx) / 2.0);
+    if (bf16) c = (double)__bfloat162float(__float2bfloat16_rn((float)c));
+    return (float)c;
+}
+
+/* 1 / (c |a_i|) with |a_i| the row length: lambda res c / ||a_i||^2 = lambda res row_scale */
+__device__ __forceinline__ float dev_row_scale(float chord, int len) { return (float)(1.0 / ((double)chord * (double)len)); }
+
 /* Fills the row slot of each history.  A sample within `margin` of a voxel
  * face has two candidate voxels; when they are exactly the previous row entry
  * and the (certain) next sample's voxel, either choice gives the same row
@@ -816,6 +847,8 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
  * next sample is written unconditionally; k_mlp_dedupe then drops the repeats
  * around the resolved entries.  With exact != 0 every sample is binary64. */
 __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const uint32_t* __restrict__ order,
+                                                  HistView h, int bf16, float* __restrict__ chord,
+                                                  float* __restrict__ row_scale,
                                                   const MlpRec* __restrict__ rec,
                                                   const uint32_t* __restrict__ first_voxel,
                                                   const float* __restrict__ x_entry, const float* __restrict__ y_entry,
@@ -828,6 +861,10 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (order) i = order[i];
+    /* the row's chord in binary64 (EffectiveChordLength_GPU): its FP64 work
+     * overlaps the other warps' binary32 samples */
+    const float cf = dev_row_chord(g, h, i, bf16);
+    chord[i] = cf;
     const MlpRec& R = rec[i];
     const double u_2 = R.m.u_2;
     const int K = dev_sample_count(tab, kmax, u_2, g.mlp_u_step);
@@ -905,6 +942,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
         }
     }
     row_len[i] = len;
+    if (!deferred) row_scale[i] = dev_row_scale(cf, len); /* rows with recomputed samples: k_mlp_dedupe */
     if (deferred) {
         unsigned long long r = atomicAdd(flags + ERR_MLP_FIXROWS, 1ull);
         fix_rows[r] = i; /* at most one entry per row: r < n */
@@ -937,6 +975,7 @@ __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __rest
 __global__ void __launch_bounds__(256) k_mlp_dedupe(int64_t rows_cap, const int64_t* __restrict__ fix_rows,
                                                     const int64_t* __restrict__ row_start, int* __restrict__ row_len,
                                                     uint32_t* __restrict__ rows, uint32_t nv,
+                                                    const float* __restrict__ chord, float* __restrict__ row_scale,
                                                     unsigned long long* __restrict__ flags) {
     int64_t count = (int64_t)flags[ERR_MLP_FIXROWS];
     if (count > rows_cap) count = rows_cap;
@@ -964,6 +1003,7 @@ __global__ void __launch_bounds__(256) k_mlp_dedupe(int64_t rows_cap, const int6
         }
         if (lane == 0) {
             row_len[i] = w;
+            row_scale[i] = dev_row_scale(chord[i], w);
             if (outside) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
         }
     }
@@ -984,21 +1024,6 @@ __global__ void k_len64(int64_t n, const int* __restrict__ len, int64_t* __restr
     if (i < n) out[i] = len[i];
 }
 
-/* EffectiveChordLength_GPU (.cu:4974-4995) with correctly rounded sinf/cosf */
-__device__ double dev_chord(const DevGeom& g, double abs_angle_t, double abs_angle_v) {
-    const double VW = g.voxel_width, VT = g.voxel_thickness, STEP = g.mlp_u_step;
-    double eff_t = abs_angle_t - ((int)(abs_angle_t / (PCT_PI / 2))) * (PCT_PI / 2);
-    double eff_v = fabs(abs_angle_v);
-    double sf = STEP / VW;
-    float s2t = pct_sinf((float)(2 * eff_t)), ct = pct_cosf((float)eff_t), st = pct_sinf((float)eff_t);
-    double c2d = (1 / 3.0) * ((sf * sf * s2t - 6) / (sf * s2t - 2 * (ct + st)) + sf * sf * s2t / (2 * (ct + st)));
-    double mean_pixel_width = VW / (ct + st);
-    double hf = VT / mean_pixel_width;
-    sf = STEP / mean_pixel_width;
-    float s2v = pct_sinf((float)(2 * eff_v)), cv = pct_cosf((float)eff_v), sv = pct_sinf((float)eff_v);
-    double c3d = (1 / 3.0) * ((sf * sf * s2v - 6 * hf) / (sf * s2v - 2 * (hf * cv + sv)) + sf * sf * s2v / (2 * (hf * cv + sv)));
-    return VW * c2d * c3d;
-}
 
 /* bf16: the chord length rounded to bfloat16 (round to nearest even), the value
  * a bf16 store holds; it then enters the row norm and the DROP updates. */
@@ -1006,12 +1031,9 @@ __global__ void k_row_norms(DevGeom g, int64_t n, HistView h, const int* __restr
                             float* __restrict__ row_scale, int bf16) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double ae = h.xy_entry_angle[i], ax = h.xy_exit_angle[i], ze = h.xz_entry_angle[i], zx = h.xz_exit_angle[i];
-    double c = dev_chord(g, (ae + ax) / 2.0, (ze + zx) / 2.0);
-    if (bf16) c = (double)__bfloat162float(__float2bfloat16_rn((float)c));
-    chord[i] = (float)c;
-    /* ||a_i||^2 = c^2 len; the DROP update is lambda res c / ||a_i||^2 = lambda res row_scale */
-    row_scale[i] = (float)(1.0 / (c * (double)len[i]));
+    const float c = dev_row_chord(g, h, i, bf16);
+    chord[i] = c;
+    row_scale[i] = dev_row_scale(c, len[i]);
 }
 
 /* Exclusive scan of int64 lengths into offsets[0..n]: per-tile sums, a scan of
@@ -1198,7 +1220,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         }
         ++c->launches;
         k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
-            c->dg, n, order, rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
+            c->dg, n, order, h, c->cfg.chord_bf16, c->chord.as<float>(), c->row_scale.as<float>(), rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
             c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(), c->mlp_queue.as<MlpDeferred>(),
             queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
         c->launches += 2;
@@ -1207,11 +1229,8 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
                                                   c->rows.as<uint32_t>());
         k_mlp_dedupe<<<8 * 152, 256, 0, c->stream>>>(n, c->mlp_fix_rows.as<int64_t>(),
                                                      c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
-                                                     c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels, flags);
-        ++c->launches;
-        k_row_norms<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, h, c->row_len.as<int>(),
-                                                                 c->chord.as<float>(), c->row_scale.as<float>(),
-                                                                 c->cfg.chord_bf16);
+                                                     c->rows.as<uint32_t>(), (uint32_t)c->geo.num_voxels,
+                                                     c->chord.as<float>(), c->row_scale.as<float>(), flags);
         PCT_CUDA(cudaGetLastError());
     }
     c->row_capacity = bound_total;
