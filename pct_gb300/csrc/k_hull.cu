@@ -519,7 +519,7 @@ __global__ void k_avg_filter(DevGeom g, int radius, double threshold, const uint
 
 }  // namespace
 
-static pct_status ensure_hull_images(pct_ctx* c) {
+pct_status pct_hull_images_ready(pct_ctx* c) {
     size_t V = (size_t)c->geo.num_voxels * 4;
     unsigned grid = pct_grid_for(c->geo.num_voxels, 256);
     if (c->cfg.sc_on && !c->sc_hull.p) {
@@ -559,33 +559,33 @@ __global__ void k_walk_key(DevGeom g, int kind, double threshold, int64_t n, con
 }
 
 /* hull_detection (.cu:3265-3273) on the staged chunk c->h2[0, n). */
-pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed) {
-    PCT_TRY(ensure_hull_images(c));
-    HistView h = c->view(c->h2);
+/* hull_detection (.cu:3265-3273) on n staged histories h (flags missed) on
+ * stream st; the images exist (pct_hull_images_ready) and c->walk_order holds
+ * at least 2 n entries (the launch order and its keys). */
+pct_status pct_hull_walk_range(pct_ctx* c, HistView h, int64_t n, const uint8_t* missed, cudaStream_t st) {
+    if (n <= 0) return PCT_OK;
     unsigned grid = pct_grid_for(n, 256);
     unsigned long long* flags = c->err_flags.as<unsigned long long>();
     const bool exact = c->cfg.walk_exact != 0;
     /* the binary32 walks run in order of walk length (warps of equal work) */
     uint32_t* order = nullptr;
     uint32_t* key = nullptr;
-    if (!exact && n > 0 && n <= (int64_t)0xffffffffu) {
-        PCT_TRY(c->walk_order.alloc(sizeof(uint32_t) * 2 * (size_t)n));
+    if (!exact && n <= (int64_t)0xffffffffu && c->walk_order.bytes >= sizeof(uint32_t) * 2 * (size_t)n) {
         order = c->walk_order.as<uint32_t>();
         key = order + n;
     }
     auto walk = [&](const DevGeom& g, int kind, double thr, int64_t nn, const uint8_t* ms, const HistView& hv, int* img,
                     unsigned long long* fl) {
         if (exact) {
-            k_hull_walk<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, img, fl);
+            k_hull_walk<<<grid, 256, 0, st>>>(g, kind, thr, nn, ms, hv, img, fl);
             return;
         }
         if (order) {
             c->launches += 2;
-            k_walk_key<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, ms, hv, key);
-            k_chunk_order<uint32_t><<<(unsigned)((nn + ORDER_CHUNK - 1) / ORDER_CHUNK), 1024, 0, c->stream>>>(nn, key,
-                                                                                                            order);
+            k_walk_key<<<grid, 256, 0, st>>>(g, kind, thr, nn, ms, hv, key);
+            k_chunk_order<uint32_t><<<(unsigned)((nn + ORDER_CHUNK - 1) / ORDER_CHUNK), 1024, 0, st>>>(nn, key, order);
         }
-        k_hull_walk_fast<<<grid, 256, 0, c->stream>>>(g, kind, thr, nn, order, ms, hv, img, fl);
+        k_hull_walk_fast<<<grid, 256, 0, st>>>(g, kind, thr, nn, order, ms, hv, img, fl);
     };
     if (c->cfg.sc_on) {
         ++c->launches;
@@ -603,9 +603,10 @@ pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed) {
     return PCT_OK;
 }
 
+
 pct_status pct_stage_hull_finish(pct_ctx* c) {
     if (c->stage != ST_BINNED) return pct_fail(PCT_ERR_STATE, "hull_detection_finish needs binned histories");
-    PCT_TRY(ensure_hull_images(c));
+    PCT_TRY(pct_hull_images_ready(c));
     const int V = c->geo.num_voxels;
     unsigned grid = pct_grid_for(V, 256);
     if (c->cfg.msc_on) {

@@ -272,7 +272,8 @@ __global__ void k_sinogram(int nb, const int* __restrict__ counts_post, const lo
 
 }  // namespace
 
-pct_status pct_hull_walk_chunk(pct_ctx* c, int64_t n, const uint8_t* missed);  /* k_hull.cu */
+pct_status pct_hull_images_ready(pct_ctx* c);                                                        /* k_hull.cu */
+pct_status pct_hull_walk_range(pct_ctx* c, HistView h, int64_t n, const uint8_t* missed, cudaStream_t st); /* k_hull.cu */
 
 namespace {
 __global__ void k_invert(const uint8_t* __restrict__ a, uint8_t* __restrict__ b, int64_t n) {
@@ -317,6 +318,8 @@ static pct_status ensure_bins(pct_ctx* c) {
     return PCT_OK;
 }
 
+constexpr int PIPE_PARTS = 4;
+
 pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], const float* angle, int64_t n,
                                    int on_dev) {
     if (c->stage > ST_BINNED) return pct_fail(PCT_ERR_STATE, "process_chunk after hull_detection_finish");
@@ -326,16 +329,15 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
     }
     PCT_TRY(ensure_tables(c));
     PCT_TRY(ensure_bins(c));
+    PCT_TRY(pct_hull_images_ready(c));
     In13 in;
     const float* d_angle = angle;
     if (!on_dev) {
         for (int k = 0; k < 13; ++k) {
             PCT_TRY(c->in13[k].alloc(sizeof(float) * n));
-            PCT_CUDA(cudaMemcpyAsync(c->in13[k].p, data13[k], sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
             in.p[k] = c->in13[k].as<float>();
         }
         PCT_TRY(c->in_angle.alloc(sizeof(float) * n));
-        PCT_CUDA(cudaMemcpyAsync(c->in_angle.p, angle, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
         d_angle = c->in_angle.as<float>();
     } else {
         for (int k = 0; k < 13; ++k) in.p[k] = data13[k];
@@ -344,14 +346,52 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
     PCT_TRY(c->tmp_missed.alloc(n * 2));
     uint8_t* missed = c->tmp_missed.as<uint8_t>();
     uint8_t* keep = missed + n;
-    HistView stage = c->view(c->h2);
-    ++c->launches;
-    k_preprocess<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(
-        c->dg, in, d_angle, n, c->trig_gantry.as<double2>(), c->trig_bins.as<double2>(), stage, missed,
-        c->bin_counts.as<int>(), c->bin_sum1.as<long long>(), 0);
-    PCT_CUDA(cudaGetLastError());
-    /* hull detection runs on the whole chunk (.cu:100) */
-    PCT_TRY(pct_hull_walk_chunk(c, n, missed));
+    const HistView stage = c->view(c->h2);
+    /* The chunk in PIPE_PARTS parts: the upload and the intersections/binning
+     * of a part on the context stream, its hull walks (hull_detection, .cu:100)
+     * on the second stream once the part is preprocessed, so that the binary32
+     * walks of one part overlap the binary64 preprocessing of the next.  The
+     * images are integer counts and the bin sums exact: the order of the parts
+     * does not change them. */
+    const int parts = n >= ((int64_t)1 << 22) ? PIPE_PARTS : 1;
+    const int64_t part = (n + parts - 1) / parts;
+    if (c->cfg.walk_exact == 0 && part <= (int64_t)0xffffffffu)
+        PCT_TRY(c->walk_order.alloc(sizeof(uint32_t) * 2 * (size_t)part));
+    cudaEvent_t ev[PIPE_PARTS + 1];
+    for (int k = 0; k <= parts; ++k) PCT_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+    pct_status st = PCT_OK;
+    for (int k = 0; k < parts && st == PCT_OK; ++k) {
+        const int64_t a = k * part, m = (a + part < n ? a + part : n) - a;
+        if (m <= 0) break;
+        In13 ink;
+        for (int j = 0; j < 13; ++j) ink.p[j] = in.p[j] + a;
+        if (!on_dev) {
+            for (int j = 0; j < 13 && st == PCT_OK; ++j)
+                if (cudaMemcpyAsync(c->in13[j].as<float>() + a, data13[j] + a, sizeof(float) * m,
+                                    cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+                    st = pct_fail(PCT_ERR_CUDA, "process_chunk: upload");
+            if (st == PCT_OK && cudaMemcpyAsync(c->in_angle.as<float>() + a, angle + a, sizeof(float) * m,
+                                                cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+                st = pct_fail(PCT_ERR_CUDA, "process_chunk: upload");
+        }
+        if (st != PCT_OK) break;
+        ++c->launches;
+        k_preprocess<<<pct_grid_for(m, 256), 256, 0, c->stream>>>(
+            c->dg, ink, d_angle + a, m, c->trig_gantry.as<double2>(), c->trig_bins.as<double2>(),
+            hv_offset(stage, a), missed + a, c->bin_counts.as<int>(), c->bin_sum1.as<long long>(), 0);
+        if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ev[k], c->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(c->stream2, ev[k], 0) != cudaSuccess) {
+            st = pct_fail(PCT_ERR_CUDA, "process_chunk: preprocessing launch");
+            break;
+        }
+        st = pct_hull_walk_range(c, hv_offset(stage, a), m, missed + a, c->stream2);
+    }
+    /* the context stream waits for the walks before the compaction */
+    if (cudaEventRecord(ev[parts], c->stream2) != cudaSuccess ||
+        cudaStreamWaitEvent(c->stream, ev[parts], 0) != cudaSuccess)
+        st = st == PCT_OK ? pct_fail(PCT_ERR_CUDA, "process_chunk: stream join") : st;
+    for (int k = 0; k <= parts; ++k) cudaEventDestroy(ev[k]);
+    PCT_TRY(st);
     /* keep = !missed (bin_num >= 0 always holds, .cu:2446) */
     PCT_TRY(pct_invert_flags(c, missed, keep, n));
     int64_t kept = 0;

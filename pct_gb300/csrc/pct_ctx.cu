@@ -278,6 +278,11 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     pct_status s = c->set_device();
     if (s == PCT_OK) {
         cudaError_t ce = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        /* the walks' stream outranks the preprocessing stream, so that walk CTAs start as
+         * preprocessing CTAs retire and the two share the SMs (binary32 and binary64 pipes) */
+        int lo = 0, hi = 0;
+        if (ce == cudaSuccess && cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) lo = hi = 0;
+        if (ce == cudaSuccess) ce = cudaStreamCreateWithPriority(&c->stream2, cudaStreamNonBlocking, hi);
         if (ce != cudaSuccess) s = pct_fail(PCT_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(ce));
     }
     if (s == PCT_OK) s = c->err_flags.alloc(sizeof(unsigned long long) * ERR_COUNT);
@@ -295,6 +300,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
     if (!c) return PCT_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->stream2) cudaStreamSynchronize(c->stream2);
     DevBuf* all[] = {&c->dense_off, &c->dense_rows, &c->row_len, &c->in_angle, &c->tmp_missed, &c->tmp_hist, &c->scan_tmp, &c->pinned_count, &c->bin_counts,
                      &c->bin_counts_post, &c->bin_sum1, &c->bin_sum2, &c->sino_sum, &c->mean_wepl, &c->mean_ut,
                      &c->mean_uv, &c->sd_wepl, &c->sd_ut, &c->sd_uv, &c->sinogram, &c->sinogram_filtered,
@@ -311,6 +317,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
     c->h.release();
     c->h2.release();
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     delete c;
     return PCT_OK;
 }

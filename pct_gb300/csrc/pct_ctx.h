@@ -113,6 +113,7 @@ struct pct_ctx {
     DevGeom dg;
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr; /* hull walks of a chunk, overlapped with its preprocessing */
     int stage = ST_EMPTY;
     int64_t launches = 0;          /* kernels launched, for pct_counts.kernel_launches */
     pct_counts counts{};
@@ -167,6 +168,14 @@ struct pct_ctx {
     }
     HistView view(HistoryStore& s) const;
 };
+
+/* The same arrays from entry `off` on. */
+inline HistView hv_offset(HistView v, int64_t off) {
+    v.x_entry += off; v.y_entry += off; v.z_entry += off; v.x_exit += off; v.y_exit += off; v.z_exit += off;
+    v.xy_entry_angle += off; v.xz_entry_angle += off; v.xy_exit_angle += off; v.xz_exit_angle += off;
+    v.wepl += off; v.bin_num += off; v.bin_valid += off; v.failed += off; v.first_voxel += off;
+    return v;
+}
 
 /* Stage implementations (one file each). */
 pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], const float* angle, int64_t n, int on_dev);

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <vector>
+#include <cuda_runtime.h>
 #include "pct_internal.h"
 
 #define PCT_TRY(call)                         \
@@ -130,27 +131,58 @@ extern "C" pct_status pct_pctd_write(const char* path, const float* const data13
     return PCT_OK;
 }
 
+/* Page-locked staging for the file uploads (freed on scope exit); empty when
+ * the allocation fails, and pageable memory is used instead. */
+struct Pinned {
+    float* p = nullptr;
+    explicit Pinned(size_t n) {
+        if (cudaMallocHost(reinterpret_cast<void**>(&p), n * sizeof(float)) != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+        }
+    }
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 /* Reads each file and uploads it as one chunk (the histories of one file share
  * the header's projection angle), like the read_data_chunk / hull_detection
- * loop of the reference driver (.cu:97-100). */
+ * loop of the reference driver (.cu:97-100).  The files are read into one
+ * page-locked buffer sized for the largest, so that the uploads run at full
+ * host-link speed; pct_process_chunk returns after the chunk's uploads have
+ * completed (its compaction synchronises the stream), so the buffer is reused. */
 extern "C" pct_status pct_process_pctd_files(pct_ctx* ctx, const char* const* paths, int num_files) {
     if (!ctx || (!paths && num_files > 0) || num_files < 0)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_process_pctd_files: bad argument");
-    std::vector<float> buf, ang;
+    int64_t nmax = 1;
+    for (int i = 0; i < num_files; ++i) {
+        int64_t n = 0;
+        PCT_TRY(pct_pctd_info(paths[i], &n, nullptr, nullptr));
+        nmax = n > nmax ? n : nmax;
+    }
+    const size_t need = (size_t)14 * (size_t)nmax; /* 13 arrays and the angles */
+    Pinned pinned(need);
+    std::vector<float> pageable;
+    float* base = pinned.p;
+    if (!base) {
+        pageable.resize(need);
+        base = pageable.data();
+    }
     for (int i = 0; i < num_files; ++i) {
         int64_t n = 0;
         float angle = 0.0f;
         PCT_TRY(pct_pctd_info(paths[i], &n, &angle, nullptr));
-        buf.resize((size_t)13 * (size_t)(n > 0 ? n : 1));
         float* d13[13];
-        for (int k = 0; k < 13; ++k) d13[k] = buf.data() + (size_t)k * (size_t)n;
+        for (int k = 0; k < 13; ++k) d13[k] = base + (size_t)k * (size_t)nmax;
         int64_t got = 0;
-        PCT_TRY(pct_pctd_read(paths[i], d13, n, &got, &angle));
+        PCT_TRY(pct_pctd_read(paths[i], d13, nmax, &got, &angle));
         if (got == 0) continue;
-        ang.assign((size_t)got, angle);
+        float* ang = base + (size_t)13 * (size_t)nmax;
+        for (int64_t j = 0; j < got; ++j) ang[j] = angle;
         const float* c13[13];
         for (int k = 0; k < 13; ++k) c13[k] = d13[k];
-        PCT_TRY(pct_process_chunk(ctx, c13, ang.data(), got, 0));
+        PCT_TRY(pct_process_chunk(ctx, c13, ang, got, 0));
     }
     return PCT_OK;
 }

@@ -116,11 +116,15 @@ class Reconstruction:
         self._call("pct_reserve", int(n))
 
     def process_chunk(self, data13, projection_angle):
-        """Host arrays: (13, n) float32 PCTD data in mm, (n,) float32 header angles."""
-        data13 = np.ascontiguousarray(data13, dtype=np.float32)
+        """Host arrays: (13, n) float32 PCTD data in mm, (n,) float32 header angles.
+        Each of the 13 rows must be contiguous, not the whole array: a column
+        slice of a larger (pinned) array is uploaded from where it lies."""
+        rows = [np.ascontiguousarray(data13[k], dtype=np.float32) for k in range(13)]
         projection_angle = np.ascontiguousarray(projection_angle, dtype=np.float32)
-        n = data13.shape[1]
-        ptrs = (C.c_void_p * 13)(*[data13[k].ctypes.data for k in range(13)])
+        n = rows[0].shape[0]
+        if any(r.shape != (n,) for r in rows) or projection_angle.shape != (n,):
+            raise ValueError("process_chunk: 13 rows and the angles must have the same length")
+        ptrs = (C.c_void_p * 13)(*[r.ctypes.data for r in rows])
         self._call("pct_process_chunk", ptrs, projection_angle.ctypes.data, n, 0)
 
     def process_pctd_files(self, paths):
