@@ -304,6 +304,7 @@ def main():
              2: "k_tile_fwd + k_tile_rows + k_tile_bwd (tiled)"}
     dom = "one DROP iteration: %s" % forms[a.drop_form]
     traffic = None
+    tr = {}
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
         tm = tr.get("drop_form_%d" % a.drop_form)
@@ -312,6 +313,34 @@ def main():
             traffic = tm["ratio_to_algorithmic"] * drop_bytes + tm["per_block_bytes"] * nblocks
     except Exception:
         pass
+
+    # The bound that applies: L2 reduction sectors.  The sectors per row entry
+    # (reductions into x_update, reads of the row stream and of the iterate)
+    # come from an ncu capture of a full block; the ceiling is measured here by
+    # pct_probe_l2 (pseudo-random float reductions into an 8 MB L2-resident
+    # array, and the same with a gather before each reduction).
+    roofline_l2 = None
+    try:
+        from pct_gb300 import _capi
+        lib = _capi.load()
+        lib.pct_probe_l2.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+        red_peak, pair_peak = C.c_double(0.0), C.c_double(0.0)
+        if lib.pct_probe_l2(local, 0, C.byref(red_peak)) == 0 and lib.pct_probe_l2(local, 1, C.byref(pair_peak)) == 0:
+            tm = tr.get("drop_form_0", {}) if a.drop_form == 0 and a.voxel_order == 0 else {}
+            spe = tm.get("l2_reduction_sectors_per_entry")
+            rpe = tm.get("l2_read_sectors_per_entry")
+            if spe and rpe:
+                red_rate = rows * spe / drop_iter_s
+                roofline_l2 = {
+                    "bound": "l2 reduction sectors", "kernel": dom, "achieved": red_rate / 1e9,
+                    "peak": red_peak.value / 1e9, "unit": "G sectors/s", "frac": red_rate / red_peak.value,
+                    "read_sectors_achieved": rows * rpe / drop_iter_s / 1e9,
+                    "peak_with_gather_before_each_reduction": pair_peak.value / 1e9,
+                    "sectors_per_entry": {"reductions": spe, "reads": rpe, "source": tm.get("l2_source")},
+                    "peak_source": "measured live: pct_probe_l2, pseudo-random red.global.add.f32 into an 8 MB "
+                                   "L2-resident array, one element per 32-byte sector"}
+    except Exception as ex:  # the probe is optional evidence; the bench line stands without it
+        roofline_l2 = {"unavailable": str(ex)[:200]}
 
     # MLP row generation, once per step: 48 B per recon history read (10 float
     # endpoint values, WEPL, first voxel) + 4 B per row entry and 4 B row length
@@ -415,7 +444,8 @@ def main():
                          "frac": achieved / hbm_peak, "traffic": traffic,
                          "algorithmic_bytes": drop_bytes,
                          "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"},
-            "roofline_mlp": {"bound": "hbm", "kernel": "MLP row generation (k_mlp_bound .. k_row_norms)",
+            "roofline_l2": roofline_l2,
+            "roofline_mlp": {"bound": "hbm", "kernel": "MLP row generation (k_mlp_bound .. k_mlp_dedupe)",
                              "achieved": mlp_achieved, "peak": hbm_peak, "unit": "GB/s",
                              "frac": mlp_achieved / hbm_peak, "algorithmic_bytes": mlp_bytes},
             "accuracy": accuracy,

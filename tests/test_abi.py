@@ -30,6 +30,13 @@ def test_c_abi_exports_every_declared_function():
     assert not missing, missing
 
 
+def test_probe_header_is_exported():
+    lib = _capi.load()
+    names = declared_functions("pct_probe.h")
+    assert names == ["pct_probe_l2"]
+    assert all(hasattr(lib, n) for n in names)
+
+
 def test_struct_layouts_match_the_library():
     from pct_gb300 import recon
     lib = _capi.load()
