@@ -730,12 +730,13 @@ struct MlpSample {
 };
 
 /* Voxel index along one axis from a binary32 coordinate; *amb is -1 / +1 when
- * the coordinate lies within `margin` of the lower / upper face of that voxel. */
-__device__ __forceinline__ int axis_index(float pos, float zero, float size, float inv_size, float margin, int* amb) {
+ * the coordinate lies within the face margin of the lower / upper face of that
+ * voxel (fractional position below flo / above fhi). */
+__device__ __forceinline__ int axis_index(float pos, float zero, float inv_size, float flo, float fhi, int* amb) {
     float q = fabsf(pos - zero) * inv_size;
     int i0 = (int)q;
     float fr = q - (float)i0;
-    *amb = fr * size < margin ? -1 : ((1.0f - fr) * size < margin ? 1 : 0);
+    *amb = fr < flo ? -1 : (fr > fhi ? 1 : 0);
     return i0;
 }
 
@@ -744,16 +745,18 @@ struct MlpFast {
     float u2_hi, u2_lo, dT, dV, T21, V21, cef, sef, x_in, y_in, V0;
 };
 
-__device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpFast& f, const MlpTableEntry te,
-                                                   float margin) {
+__device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpFast& f, const MlpTableEntry te) {
     const float X0 = g.fx0, Y0 = g.fy0, Z0 = g.fz0;
-    const float VW = g.fvw, VH = g.fvh, VT = g.fvt;
     const float iVW = g.fivw, iVH = g.fivh, iVT = g.fivt;
-    const float lnX0 = __logf(36.08f);
     const float* b = f.b;
     float d = (f.u2_hi - te.u1_hi) + (f.u2_lo - te.u1_lo);
-    float k2 = 13.6f * (1.0f + 0.038f * (__logf(d) - lnX0));
-    float c2 = k2 * k2 * (1.0f / 36.08f);
+    /* k2 / sqrt(X0) = (E0 / sqrt(X0)) (1 + 0.038 ln(d / X0)) with E0 = 13.6 MeV and
+     * X0 = 36.08 cm, as one FMA on log2(d): KA = (E0 / sqrt(X0)) 0.038 ln 2,
+     * KB = (E0 / sqrt(X0)) (1 - 0.038 ln X0), evaluated in binary64 */
+    constexpr float KA = 5.963685076e-02f;
+    constexpr float KB = 1.955643309e+00f;
+    const float ks = fmaf(KA, __log2f(d), KB);
+    float c2 = ks * ks;
     /* the terms p_m = b_m d^m once, then each moment as a fixed-weight sum of them */
     const float d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
     const float p0 = b[0], p1 = b[1] * d, p2 = b[2] * d2, p3 = b[3] * d3, p4 = b[4] * d4, p5 = b[5] * d5;
@@ -771,12 +774,12 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     /* approximate reciprocals (2 ulp): far inside the face margin that certifies each voxel */
     float inv = __fdividef(1.0f, c2 * D);
     float id = __fdividef(1.0f, d);
-    float id2 = id * id, id3 = id2 * id;
-    float Aa = Q1 * inv * id3;      /* (Sigma_2^-1)_00 */
-    float Bm = E1 * inv * id2;      /* (R1^T Sigma_2^-1 R1)_01 */
-    float Cm = E2 * inv * id;       /* (R1^T Sigma_2^-1 R1)_11 */
-    float bb = -Q2 * inv * id2;     /* (Sigma_2^-1)_01 */
-    float e3 = -E3 * inv * id;      /* d (Sigma_2^-1)_01 + (Sigma_2^-1)_11 */
+    float i1 = inv * id, i2 = i1 * id, i3 = i2 * id; /* inv / d^k */
+    float Aa = Q1 * i3;      /* (Sigma_2^-1)_00 */
+    float Bm = E1 * i2;      /* (R1^T Sigma_2^-1 R1)_01 */
+    float Cm = E2 * i1;      /* (R1^T Sigma_2^-1 R1)_11 */
+    float bb = -Q2 * i2;     /* (Sigma_2^-1)_01 */
+    float e3 = -E3 * i1;     /* d (Sigma_2^-1)_01 + (Sigma_2^-1)_11 */
     float ft0 = te.s1i0 + Aa, ft1 = te.s1i1 + Bm, ft3 = te.s1i3 + Cm;
     float idet = __fdividef(1.0f, fmaf(ft0, ft3, -ft1 * ft1));
     float beta = fmaf(ft3, Aa, -ft1 * Bm) * idet;
@@ -794,9 +797,9 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
         return s;
     }
     int ax, ay, az;
-    int vx = axis_index(x1, X0, VW, iVW, margin, &ax);
-    int vy = axis_index(y1, Y0, VH, iVH, margin, &ay);
-    int vz = axis_index(z1, Z0, VT, iVT, margin, &az);
+    int vx = axis_index(x1, X0, iVW, g.fmlo_x, g.fmhi_x, &ax);
+    int vy = axis_index(y1, Y0, iVH, g.fmlo_y, g.fmhi_y, &ay);
+    int vz = axis_index(z1, Z0, iVT, g.fmlo_z, g.fmhi_z, &az);
     const int C = g.columns, CR = g.columns * g.rows;
     s.v = (uint32_t)(vx + vy * C + vz * CR);
     int namb = (ax != 0) + (ay != 0) + (az != 0);
@@ -852,8 +855,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
                                                   const MlpRec* __restrict__ rec,
                                                   const uint32_t* __restrict__ first_voxel,
                                                   const float* __restrict__ x_entry, const float* __restrict__ y_entry,
-                                                  const MlpTableEntry* __restrict__ tab, int kmax, float margin,
-                                                  int exact, const int64_t* __restrict__ row_start,
+                                                  const MlpTableEntry* __restrict__ tab, int kmax, int exact, const int64_t* __restrict__ row_start,
                                                   uint32_t* __restrict__ rows, int* __restrict__ row_len,
                                                   MlpDeferred* __restrict__ queue, int64_t queue_cap,
                                                   int64_t* __restrict__ fix_rows,
@@ -900,10 +902,10 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
         f.y_in = y_entry[i];
         f.V0 = (float)R.m.V0;
         int force = 0; /* the last entry is a placeholder: write the next voxel whatever it is */
-        MlpSample cur = K > 0 ? dev_mlp_sample(g, f, tab[0], margin) : MlpSample{SAMPLE_CERTAIN, 0u, 0u};
+        MlpSample cur = K > 0 ? dev_mlp_sample(g, f, tab[0]) : MlpSample{SAMPLE_CERTAIN, 0u, 0u};
         for (int k = 0; k < K; ++k) {
             MlpSample nxt{SAMPLE_EXACT, 0u, 0u};
-            if (k + 1 < K) nxt = dev_mlp_sample(g, f, tab[k + 1], margin);
+            if (k + 1 < K) nxt = dev_mlp_sample(g, f, tab[k + 1]);
             if (cur.state == SAMPLE_CERTAIN) {
                 if (force || cur.v != prev) {
                     rows[out + len++] = dev_to_brick(g, cur.v);
@@ -1209,7 +1211,6 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         PCT_TRY(pct_scan_lengths(c, c->mlp_bound.as<int64_t>(), n, c->row_offsets.as<int64_t>(), &bound_total));
         PCT_TRY(c->rows.alloc(sizeof(uint32_t) * (bound_total > 0 ? bound_total : 1)));
         const int exact = c->cfg.mlp_exact != 0;
-        const float margin = (float)c->cfg.mlp_face_margin;
         uint32_t* order = nullptr;
         if (n <= (int64_t)0xffffffffu) {
             PCT_TRY(c->mlp_order.alloc(sizeof(uint32_t) * n));
@@ -1220,7 +1221,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         }
         ++c->launches;
         k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
-            c->dg, n, order, h, c->cfg.chord_bf16, c->chord.as<float>(), c->row_scale.as<float>(), rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, margin, exact,
+            c->dg, n, order, h, c->cfg.chord_bf16, c->chord.as<float>(), c->row_scale.as<float>(), rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, exact,
             c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(), c->mlp_queue.as<MlpDeferred>(),
             queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
         c->launches += 2;

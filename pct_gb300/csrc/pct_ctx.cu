@@ -98,6 +98,12 @@ DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g) {
     d.fx0 = (float)g.x_zero; d.fy0 = (float)g.y_zero; d.fz0 = (float)g.z_zero;
     d.fvw = (float)g.voxel_width; d.fvh = (float)g.voxel_height; d.fvt = (float)g.voxel_thickness;
     d.fivw = 1.0f / d.fvw; d.fivh = 1.0f / d.fvh; d.fivt = 1.0f / d.fvt; /* IEEE quotients, as on the device */
+    auto up = [](double q) { float f = (float)q; return (double)f < q ? std::nextafter(f, INFINITY) : f; };
+    auto down = [](double q) { float f = (float)q; return (double)f > q ? std::nextafter(f, -INFINITY) : f; };
+    const double m = c.mlp_face_margin;
+    d.fmlo_x = up(m / g.voxel_width); d.fmlo_y = up(m / g.voxel_height); d.fmlo_z = up(m / g.voxel_thickness);
+    d.fmhi_x = down(1.0 - m / g.voxel_width); d.fmhi_y = down(1.0 - m / g.voxel_height);
+    d.fmhi_z = down(1.0 - m / g.voxel_thickness);
     return d;
 }
 

@@ -81,6 +81,10 @@ struct DevGeom {
     /* binary32 copies for the binary32 walks and MLP samples (a conversion in the
      * kernel would run on the FP64 pipe at every use) */
     float fx0, fy0, fz0, fvw, fvh, fvt, fivw, fivh, fivt;
+    /* the MLP face margin as a fraction of each voxel size: a binary32 sample
+     * whose fractional position along an axis is below flo or above fhi is
+     * recomputed in binary64 (rounded outwards from mlp_face_margin / size) */
+    float fmlo_x, fmlo_y, fmlo_z, fmhi_x, fmhi_y, fmhi_z;
 };
 
 enum Stage {
