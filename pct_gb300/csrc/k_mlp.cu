@@ -740,6 +740,17 @@ __device__ __forceinline__ int axis_index(float pos, float zero, float inv_size,
     return i0;
 }
 
+/* The row entry of voxel (vx, vy, vz) in the rows' voxel order: the brick
+ * index formed directly inside the grid; outside it the reference's linear
+ * index vx + vy C + vz C R (which wraps into a neighbouring row or slice),
+ * mapped as every other linear index is. */
+__device__ __forceinline__ uint32_t row_entry(const DevGeom& g, int vx, int vy, int vz) {
+    if (g.brick && (unsigned)vx < (unsigned)g.columns && (unsigned)vy < (unsigned)g.rows &&
+        (unsigned)vz < (unsigned)g.slices)
+        return dev_brick_xyz((uint32_t)g.columns, (uint32_t)g.rows, (uint32_t)vx, (uint32_t)vy, (uint32_t)vz);
+    return dev_to_brick(g, (uint32_t)(vx + vy * g.columns + vz * g.columns * g.rows));
+}
+
 struct MlpFast {
     float b[6];
     float u2_hi, u2_lo, dT, dV, T21, V21, cef, sef, x_in, y_in, V0;
@@ -800,14 +811,13 @@ __device__ __forceinline__ MlpSample dev_mlp_sample(const DevGeom& g, const MlpF
     int vx = axis_index(x1, X0, iVW, g.fmlo_x, g.fmhi_x, &ax);
     int vy = axis_index(y1, Y0, iVH, g.fmlo_y, g.fmhi_y, &ay);
     int vz = axis_index(z1, Z0, iVT, g.fmlo_z, g.fmhi_z, &az);
-    const int C = g.columns, CR = g.columns * g.rows;
-    s.v = (uint32_t)(vx + vy * C + vz * CR);
+    s.v = row_entry(g, vx, vy, vz); /* voxels as row entries (the rows' voxel order) */
     int namb = (ax != 0) + (ay != 0) + (az != 0);
     if (namb == 0) {
         s.state = SAMPLE_CERTAIN;
     } else if (namb == 1) {
         s.state = SAMPLE_PAIR;
-        s.v_alt = (uint32_t)((vx + ax) + (vy + ay) * C + (vz + az) * CR);
+        s.v_alt = row_entry(g, vx + ax, vy + ay, vz + az);
     } else {
         s.state = SAMPLE_EXACT;
     }
@@ -873,15 +883,15 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
     const uint32_t nv = (uint32_t)g.num_voxels;
     int64_t out = row_start[i];
     int len = 0;
-    uint32_t prev = first_voxel[i];
-    rows[out + len++] = dev_to_brick(g, prev);
+    uint32_t prev = dev_to_brick(g, first_voxel[i]); /* row entries: the rows' voxel order */
+    rows[out + len++] = prev;
     int fp64_samples = 0, deferred = 0, outside = prev >= nv;
     if (exact) {
         for (int k = 0; k < K; ++k) {
-            uint32_t v = dev_mlp_voxel_rec(g, &R, tab[k].u1);
+            uint32_t v = dev_to_brick(g, dev_mlp_voxel_rec(g, &R, tab[k].u1));
             ++fp64_samples;
             if (v != prev) {
-                rows[out + len++] = dev_to_brick(g, v);
+                rows[out + len++] = v;
                 prev = v;
                 outside += v >= nv;
             }
@@ -908,7 +918,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
             if (k + 1 < K) nxt = dev_mlp_sample(g, f, tab[k + 1]);
             if (cur.state == SAMPLE_CERTAIN) {
                 if (force || cur.v != prev) {
-                    rows[out + len++] = dev_to_brick(g, cur.v);
+                    rows[out + len++] = cur.v;
                     prev = cur.v;
                     outside += cur.v >= nv;
                     force = 0;
@@ -931,9 +941,9 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
                     force = 1;
                 } else {
                     /* queue full: binary64 here */
-                    uint32_t v = dev_mlp_voxel_rec(g, &R, tab[k].u1);
+                    uint32_t v = dev_to_brick(g, dev_mlp_voxel_rec(g, &R, tab[k].u1));
                     if (force || v != prev) {
-                        rows[out + len++] = dev_to_brick(g, v);
+                        rows[out + len++] = v;
                         prev = v;
                         outside += v >= nv;
                         force = 0;
