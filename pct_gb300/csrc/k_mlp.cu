@@ -865,7 +865,8 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
                                                   const MlpRec* __restrict__ rec,
                                                   const uint32_t* __restrict__ first_voxel,
                                                   const float* __restrict__ x_entry, const float* __restrict__ y_entry,
-                                                  const MlpTableEntry* __restrict__ tab, int kmax, int exact, const int64_t* __restrict__ row_start,
+                                                  const MlpTableEntry* __restrict__ tab,
+                                                  const int64_t* __restrict__ bound, int exact, const int64_t* __restrict__ row_start,
                                                   uint32_t* __restrict__ rows, int* __restrict__ row_len,
                                                   MlpDeferred* __restrict__ queue, int64_t queue_cap,
                                                   int64_t* __restrict__ fix_rows,
@@ -879,13 +880,14 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
     chord[i] = cf;
     const MlpRec& R = rec[i];
     const double u_2 = R.m.u_2;
-    const int K = dev_sample_count(tab, kmax, u_2, g.mlp_u_step);
+    const int K = (int)(bound[i] - 1); /* dev_sample_count, stored by k_mlp_bound */
     const uint32_t nv = (uint32_t)g.num_voxels;
     int64_t out = row_start[i];
     int len = 0;
     uint32_t prev = dev_to_brick(g, first_voxel[i]); /* row entries: the rows' voxel order */
     rows[out + len++] = prev;
     int fp64_samples = 0, deferred = 0, outside = prev >= nv;
+    int first_def = 0, outside_pre = 0; /* entry of the first placeholder, outside entries before it */
     if (exact) {
         for (int k = 0; k < K; ++k) {
             uint32_t v = dev_to_brick(g, dev_mlp_voxel_rec(g, &R, tab[k].u1));
@@ -930,6 +932,10 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
                 ++fp64_samples;
                 unsigned long long slot = atomicAdd(flags + ERR_MLP_QUEUED, 1ull);
                 if ((int64_t)slot < queue_cap) {
+                    if (!deferred) {
+                        first_def = len;
+                        outside_pre = outside;
+                    }
                     MlpDeferred q;
                     q.pos = out + len;
                     q.hist = i;
@@ -957,7 +963,8 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
     if (!deferred) row_scale[i] = dev_row_scale(cf, len); /* rows with recomputed samples: k_mlp_dedupe */
     if (deferred) {
         unsigned long long r = atomicAdd(flags + ERR_MLP_FIXROWS, 1ull);
-        fix_rows[r] = i; /* at most one entry per row: r < n */
+        fix_rows[r] = i | ((int64_t)first_def << 40); /* at most one entry per row: r < n */
+        if (outside_pre) atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside_pre);
     } else if (outside) {
         atomicAdd(flags + ERR_ROWS_OUTSIDE, (unsigned long long)outside);
     }
@@ -980,10 +987,13 @@ __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __rest
 }
 
 /* Drops consecutive repeats in the rows that had queued samples, one warp per
- * row.  An entry is kept when it differs from the entry before it (the last
- * kept value always equals that entry), and kept entries are compacted in
- * place: each 32-entry chunk is read into registers before any lane writes,
- * and writes never pass the chunk being read. */
+ * row, from the row's first placeholder on (fix_rows holds the history in its
+ * low 40 bits and that entry above them; the entries before it are final and
+ * their outside-the-grid count is already recorded).  An entry is kept when
+ * it differs from the entry before it (the last kept value always equals that
+ * entry), and kept entries are compacted in place: each 32-entry chunk is read
+ * into registers before any lane writes, and writes never pass the chunk being
+ * read. */
 __global__ void __launch_bounds__(256) k_mlp_dedupe(int64_t rows_cap, const int64_t* __restrict__ fix_rows,
                                                     const int64_t* __restrict__ row_start, int* __restrict__ row_len,
                                                     uint32_t* __restrict__ rows, uint32_t nv,
@@ -994,12 +1004,14 @@ __global__ void __launch_bounds__(256) k_mlp_dedupe(int64_t rows_cap, const int6
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < count; r += warps) {
-        const int64_t i = fix_rows[r];
+        const int64_t packed = fix_rows[r];
+        const int64_t i = packed & ((1ll << 40) - 1);
+        const int b0 = (int)(packed >> 40); /* >= 1: entry 0 is the first voxel */
         uint32_t* row = rows + row_start[i];
         const int len = row_len[i];
-        int w = 0, outside = 0;
-        uint32_t last = 0; /* entry base - 1 */
-        for (int base = 0; base < len; base += 32) {
+        int w = b0, outside = 0;
+        uint32_t last = row[b0 - 1]; /* entry base - 1 */
+        for (int base = b0; base < len; base += 32) {
             const int j = base + lane;
             const uint32_t v = j < len ? row[j] : 0u;
             uint32_t before = __shfl_up_sync(0xffffffffu, v, 1);
@@ -1231,7 +1243,7 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
         }
         ++c->launches;
         k_mlp_fast<<<pct_grid_for(n, 128), 128, 0, c->stream>>>(
-            c->dg, n, order, h, c->cfg.chord_bf16, c->chord.as<float>(), c->row_scale.as<float>(), rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), kmax, exact,
+            c->dg, n, order, h, c->cfg.chord_bf16, c->chord.as<float>(), c->row_scale.as<float>(), rec, h.first_voxel, h.x_entry, h.y_entry, c->mlp_table.as<MlpTableEntry>(), c->mlp_bound.as<int64_t>(), exact,
             c->row_offsets.as<int64_t>(), c->rows.as<uint32_t>(), c->row_len.as<int>(), c->mlp_queue.as<MlpDeferred>(),
             queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
         c->launches += 2;
