@@ -550,24 +550,40 @@ __device__ __forceinline__ void dev_mlp_setup(const HistView& h, int64_t i, MlpS
     m.pre3 = u_2 * (A0 + u_2 * (AL(1, 2) + u_2 * (AL(2, 3) + u_2 * (AL(3, 4) + u_2 * (AL(4, 5) + AU(u_2, 5, 6))))));
 }
 
-/* One MLP sample at depth u_1 in binary64, the reference's operation order. */
-__device__ __forceinline__ int dev_mlp_voxel(const DevGeom& g, const MlpSetup& m, double u_1) {
-    const double u_0 = 0.0, u_2 = m.u_2;
-    double R0_1 = u_1, R1_1 = u_2 - u_1, R1T_2 = u_2 - u_1;
-    const double R0_0 = 1.0, R0_2 = 0.0, R0_3 = 1.0, R1_0 = 1.0, R1_2 = 0.0, R1_3 = 1.0;
-    const double R1T_0 = 1.0, R1T_1 = 0.0, R1T_3 = 1.0;
+/* The terms of an MLP sample that depend on its depth u_1 alone (the entry
+ * side Sigma_1^-1 and the exit side's polynomials in u_1), binary64. */
+struct MlpDepthTerms {
+    double S1I0, S1I1, S1I3, cst1, cst2, cst3;
+};
+
+__device__ __forceinline__ void dev_mlp_depth_terms(double u_1, MlpDepthTerms& t) {
+    const double u_0 = 0.0;
     double k1 = PCT_E_0 * (1 + 0.038 * pct_log((u_1 - u_0) / PCT_X_0));
     double c1 = k1 * k1 / PCT_X_0;
     double st1 = c1 * (pct_cube(u_1) * (AL(0, 3) + u_1 * (AL(1, 12) + u_1 * (AL(2, 30) + u_1 * (AL(3, 60) + u_1 * (AL(4, 105) + AU(u_1, 5, 168)))))));
     double stt1 = c1 * ((u_1 * u_1) * (AL(0, 2) + u_1 * (AL(1, 6) + u_1 * (AL(2, 12) + u_1 * (AL(3, 20) + u_1 * (AL(4, 30) + AU(u_1, 5, 42)))))));
     double sth1 = c1 * (u_1 * (A0 + u_1 * (AL(1, 2) + u_1 * (AL(2, 3) + u_1 * (AL(3, 4) + u_1 * (AL(4, 5) + AU(u_1, 5, 6)))))));
     double det1 = st1 * sth1 - stt1 * stt1;
-    double S1I0 = sth1 / det1, S1I1 = -stt1 / det1, S1I2 = -stt1 / det1, S1I3 = st1 / det1;
+    t.S1I0 = sth1 / det1;
+    t.S1I1 = -stt1 / det1; /* = S1I2 */
+    t.S1I3 = st1 / det1;
+    t.cst1 = u_1 * (A0 + u_1 * (AL(1, 2) + u_1 * (AL(2, 3) + u_1 * (AL(3, 4) + u_1 * (AL(4, 5) + AU(u_1, 5, 6))))));
+    t.cst2 = (u_1 * u_1) * (AL(0, 2) + u_1 * (AL(1, 3) + u_1 * (AL(2, 4) + u_1 * (AL(3, 5) + u_1 * (AL(4, 6) + AU(u_1, 5, 7))))));
+    t.cst3 = pct_cube(u_1) * (AL(0, 3) + u_1 * (AL(1, 4) + u_1 * (AL(2, 5) + u_1 * (AL(3, 6) + u_1 * (AL(4, 7) + AU(u_1, 5, 8))))));
+}
+
+/* One MLP sample at depth u_1 in binary64, the reference's operation order,
+ * from its depth terms. */
+__device__ __forceinline__ int dev_mlp_voxel_terms(const DevGeom& g, const MlpSetup& m, double u_1,
+                                                   const MlpDepthTerms& t) {
+    const double u_2 = m.u_2;
+    double R0_1 = u_1, R1_1 = u_2 - u_1, R1T_2 = u_2 - u_1;
+    const double R0_0 = 1.0, R0_2 = 0.0, R0_3 = 1.0, R1_0 = 1.0, R1_2 = 0.0, R1_3 = 1.0;
+    const double R1T_0 = 1.0, R1T_1 = 0.0, R1T_3 = 1.0;
+    const double S1I0 = t.S1I0, S1I1 = t.S1I1, S1I2 = t.S1I1, S1I3 = t.S1I3;
+    const double cst1 = t.cst1, cst2 = t.cst2, cst3 = t.cst3;
     double k2 = PCT_E_0 * (1 + 0.038 * pct_log((u_2 - u_1) / PCT_X_0));
     double c2 = k2 * k2 / PCT_X_0;
-    double cst1 = u_1 * (A0 + u_1 * (AL(1, 2) + u_1 * (AL(2, 3) + u_1 * (AL(3, 4) + u_1 * (AL(4, 5) + AU(u_1, 5, 6))))));
-    double cst2 = (u_1 * u_1) * (AL(0, 2) + u_1 * (AL(1, 3) + u_1 * (AL(2, 4) + u_1 * (AL(3, 5) + u_1 * (AL(4, 6) + AU(u_1, 5, 7))))));
-    double cst3 = pct_cube(u_1) * (AL(0, 3) + u_1 * (AL(1, 4) + u_1 * (AL(2, 5) + u_1 * (AL(3, 6) + u_1 * (AL(4, 7) + AU(u_1, 5, 8))))));
     double st2 = c2 * (m.pre1 - (u_2 * u_2) * cst1 + 2 * u_2 * cst2 - cst3);
     double stt2 = c2 * (m.pre2 - u_2 * cst1 + cst2);
     double sth2 = c2 * (m.pre3 - cst1);
@@ -612,6 +628,12 @@ __device__ __forceinline__ int dev_mlp_voxel(const DevGeom& g, const MlpSetup& m
     return vx + vy * g.columns + vz * g.columns * g.rows;
 }
 
+__device__ __forceinline__ int dev_mlp_voxel(const DevGeom& g, const MlpSetup& m, double u_1) {
+    MlpDepthTerms t;
+    dev_mlp_depth_terms(u_1, t);
+    return dev_mlp_voxel_terms(g, m, u_1, t);
+}
+
 /* ---- binary32 fast path ------------------------------------------------------
  * With s = u_2 - u the scattering moments of the exit side are polynomials in
  * d = u_2 - u_1 with positive weights (no cancellation):
@@ -641,19 +663,18 @@ __global__ void k_mlp_u1(double step, int K, MlpTableEntry* __restrict__ tab) {
     }
 }
 
-__global__ void k_mlp_table(int K, MlpTableEntry* __restrict__ tab) {
+/* Per sample index k: the binary32 entry and the binary64 depth terms (for the
+ * samples recomputed in binary64 by k_mlp_fix). */
+__global__ void k_mlp_table(int K, MlpTableEntry* __restrict__ tab, MlpDepthTerms* __restrict__ terms) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     double u_1 = tab[k].u1;
-    double k1 = PCT_E_0 * (1 + 0.038 * pct_log(u_1 / PCT_X_0));
-    double c1 = k1 * k1 / PCT_X_0;
-    double st1 = c1 * (pct_cube(u_1) * (AL(0, 3) + u_1 * (AL(1, 12) + u_1 * (AL(2, 30) + u_1 * (AL(3, 60) + u_1 * (AL(4, 105) + AU(u_1, 5, 168)))))));
-    double stt1 = c1 * ((u_1 * u_1) * (AL(0, 2) + u_1 * (AL(1, 6) + u_1 * (AL(2, 12) + u_1 * (AL(3, 20) + u_1 * (AL(4, 30) + AU(u_1, 5, 42)))))));
-    double sth1 = c1 * (u_1 * (A0 + u_1 * (AL(1, 2) + u_1 * (AL(2, 3) + u_1 * (AL(3, 4) + u_1 * (AL(4, 5) + AU(u_1, 5, 6)))))));
-    double det1 = st1 * sth1 - stt1 * stt1;
-    tab[k].s1i0 = (float)(sth1 / det1);
-    tab[k].s1i1 = (float)(-stt1 / det1);
-    tab[k].s1i3 = (float)(st1 / det1);
+    MlpDepthTerms t;
+    dev_mlp_depth_terms(u_1, t);
+    terms[k] = t;
+    tab[k].s1i0 = (float)t.S1I0;
+    tab[k].s1i1 = (float)t.S1I1;
+    tab[k].s1i3 = (float)t.S1I3;
     float hi = (float)u_1;
     tab[k].u1_hi = hi;
     tab[k].u1_lo = (float)(u_1 - (double)hi);
@@ -700,13 +721,16 @@ __global__ void __launch_bounds__(256) k_mlp_bound(DevGeom g, int64_t n, HistVie
     /* Taylor coefficients of the scattering power around u_2 (binary64, then float) */
     const double A[6] = {A0, PCT_A1_M * PCT_A1_P, PCT_A2_M * PCT_A2_P, PCT_A3_M * PCT_A3_P, PCT_A4_M * PCT_A4_P,
                          PCT_A5_M * PCT_A5_P};
+    /* binomial coefficients C(k, mm): the exact integers of binom * (k + 1) / (k + 1 - mm) */
+    const double BINOM[6][6] = {{1, 1, 1, 1, 1, 1},  {0, 1, 2, 3, 4, 5},   {0, 0, 1, 3, 6, 10},
+                                {0, 0, 0, 1, 4, 10}, {0, 0, 0, 0, 1, 5},   {0, 0, 0, 0, 0, 1}};
 #pragma unroll
     for (int mm = 0; mm < 6; ++mm) {
-        double sum = 0.0, up = 1.0, binom = 1.0;
+        double sum = 0.0, up = 1.0;
+#pragma unroll
         for (int k = mm; k < 6; ++k) {
-            sum += binom * A[k] * up;
+            sum += BINOM[mm][k] * A[k] * up;
             up *= r.m.u_2;
-            binom = binom * (k + 1) / (k + 1 - mm);
         }
         r.b[mm] = (float)((mm & 1) ? -sum : sum);
     }
@@ -974,6 +998,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const
 /* The queued samples in binary64, one thread each. */
 __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __restrict__ rec,
                                                  const MlpTableEntry* __restrict__ tab,
+                                                 const MlpDepthTerms* __restrict__ terms,
                                                  const MlpDeferred* __restrict__ queue, int64_t queue_cap,
                                                  const unsigned long long* __restrict__ flags,
                                                  uint32_t* __restrict__ rows) {
@@ -982,7 +1007,8 @@ __global__ void __launch_bounds__(128) k_mlp_fix(DevGeom g, const MlpRec* __rest
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
         MlpDeferred d = queue[q];
         MlpSetup m = rec[d.hist].m;
-        rows[d.pos] = dev_to_brick(g, (uint32_t)dev_mlp_voxel(g, m, tab[d.k].u1));
+        /* the depth terms of sample d.k come from the table: the same binary64 values */
+        rows[d.pos] = dev_to_brick(g, (uint32_t)dev_mlp_voxel_terms(g, m, tab[d.k].u1, terms[d.k]));
     }
 }
 
@@ -1190,16 +1216,21 @@ pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* 
     return PCT_OK;
 }
 
+static MlpDepthTerms* mlp_depth_terms(pct_ctx* c, int K) {
+    return reinterpret_cast<MlpDepthTerms*>(c->mlp_table.as<MlpTableEntry>() + K);
+}
+
 static pct_status ensure_mlp_table(pct_ctx* c, int* kmax) {
     const int K = 8 * (c->geo.columns + c->geo.rows + c->geo.slices) + 64;
     *kmax = K;
     if (c->mlp_table.p) return PCT_OK;
-    PCT_TRY(c->mlp_table.alloc(sizeof(MlpTableEntry) * K));
+    /* K binary32 entries, then K binary64 depth terms (mlp_depth_terms) */
+    PCT_TRY(c->mlp_table.alloc((sizeof(MlpTableEntry) + sizeof(MlpDepthTerms)) * K));
     MlpTableEntry* tab = c->mlp_table.as<MlpTableEntry>();
     ++c->launches;
     k_mlp_u1<<<1, 1, 0, c->stream>>>(c->geo.mlp_u_step, K, tab);
     ++c->launches;
-    k_mlp_table<<<pct_grid_for(K, 128), 128, 0, c->stream>>>(K, tab);
+    k_mlp_table<<<pct_grid_for(K, 128), 128, 0, c->stream>>>(K, tab, mlp_depth_terms(c, K));
     PCT_CUDA(cudaGetLastError());
     return PCT_OK;
 }
@@ -1248,7 +1279,8 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
             queue_cap, c->mlp_fix_rows.as<int64_t>(), flags);
         c->launches += 2;
         k_mlp_fix<<<4 * 152, 128, 0, c->stream>>>(c->dg, rec, c->mlp_table.as<MlpTableEntry>(),
-                                                  c->mlp_queue.as<MlpDeferred>(), queue_cap, flags,
+                                                  mlp_depth_terms(c, kmax), c->mlp_queue.as<MlpDeferred>(),
+                                                  queue_cap, flags,
                                                   c->rows.as<uint32_t>());
         k_mlp_dedupe<<<8 * 152, 256, 0, c->stream>>>(n, c->mlp_fix_rows.as<int64_t>(),
                                                      c->row_offsets.as<int64_t>(), c->row_len.as<int>(),
