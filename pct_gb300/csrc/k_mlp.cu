@@ -519,21 +519,37 @@ __device__ __forceinline__ void dev_mlp_setup(const HistView& h, int64_t i, MlpS
     double x_out = h.x_exit[i], y_out = h.y_exit[i], z_out = h.z_exit[i];
     double xy_entry = h.xy_entry_angle[i], xy_exit = h.xy_exit_angle[i];
     double xz_entry = h.xz_entry_angle[i], xz_exit = h.xz_exit_angle[i];
-    double ce = pct_cos(xy_entry), se = pct_sin(xy_entry);
+    /* The reference turns the entry direction by pi when u_in > u_out.  That
+     * comparison is made in binary32 when its margin is wide (then only the
+     * kept direction's binary64 sine and cosine are formed), else as the
+     * reference makes it. */
+    const float dxf = (float)(x_in - x_out), dyf = (float)(y_in - y_out);
+    float sf, cf;
+    sincosf((float)xy_entry, &sf, &cf);
+    const float duf = cf * dxf + sf * dyf; /* u_in - u_out */
+    const float tol = 1e-4f * (fabsf(dxf) + fabsf(dyf)) + 1e-5f;
+    int flip;
+    double ce, se;
+    if (duf > tol || duf < -tol) {
+        flip = duf > 0.0f;
+        if (flip) {
+            xy_entry += PCT_PI;
+            xy_exit += PCT_PI;
+        }
+        pct_sincos(xy_entry, &se, &ce);
+    } else {
+        pct_sincos(xy_entry, &se, &ce);
+        flip = ((ce * x_in) + (se * y_in)) > ((ce * x_out) + (se * y_out));
+        if (flip) {
+            xy_entry += PCT_PI;
+            xy_exit += PCT_PI;
+            pct_sincos(xy_entry, &se, &ce);
+        }
+    }
     double u_in = (ce * x_in) + (se * y_in);
     double u_out = (ce * x_out) + (se * y_out);
     double t_in = (ce * y_in) - (se * x_in);
     double t_out = (ce * y_out) - (se * x_out);
-    if (u_in > u_out) {
-        xy_entry += PCT_PI;
-        xy_exit += PCT_PI;
-        ce = pct_cos(xy_entry);
-        se = pct_sin(xy_entry);
-        u_in = (ce * x_in) + (se * y_in);
-        u_out = (ce * x_out) + (se * y_out);
-        t_in = (ce * y_in) - (se * x_in);
-        t_out = (ce * y_out) - (se * x_out);
-    }
     m.ce = ce;
     m.se = se;
     m.u_in = u_in;
@@ -721,19 +737,17 @@ __global__ void __launch_bounds__(256) k_mlp_bound(DevGeom g, int64_t n, HistVie
     /* Taylor coefficients of the scattering power around u_2 (binary64, then float) */
     const double A[6] = {A0, PCT_A1_M * PCT_A1_P, PCT_A2_M * PCT_A2_P, PCT_A3_M * PCT_A3_P, PCT_A4_M * PCT_A4_P,
                          PCT_A5_M * PCT_A5_P};
-    /* binomial coefficients C(k, mm): the exact integers of binom * (k + 1) / (k + 1 - mm) */
-    const double BINOM[6][6] = {{1, 1, 1, 1, 1, 1},  {0, 1, 2, 3, 4, 5},   {0, 0, 1, 3, 6, 10},
-                                {0, 0, 0, 1, 4, 10}, {0, 0, 0, 0, 1, 5},   {0, 0, 0, 0, 0, 1}};
+    /* the shift to u_2 by repeated synthetic division: afterwards
+     * c[mm] = sum_k C(k, mm) A_k u_2^(k - mm) */
+    double c[6];
 #pragma unroll
-    for (int mm = 0; mm < 6; ++mm) {
-        double sum = 0.0, up = 1.0;
+    for (int k = 0; k < 6; ++k) c[k] = A[k];
 #pragma unroll
-        for (int k = mm; k < 6; ++k) {
-            sum += BINOM[mm][k] * A[k] * up;
-            up *= r.m.u_2;
-        }
-        r.b[mm] = (float)((mm & 1) ? -sum : sum);
-    }
+    for (int mm = 0; mm < 5; ++mm)
+#pragma unroll
+        for (int k = 4; k >= mm; --k) c[k] = fma(r.m.u_2, c[k + 1], c[k]);
+#pragma unroll
+    for (int mm = 0; mm < 6; ++mm) r.b[mm] = (float)((mm & 1) ? -c[mm] : c[mm]);
     rec[i] = r;
 }
 
@@ -883,7 +897,7 @@ __device__ __forceinline__ float dev_row_scale(float chord, int len) { return (f
  * uncertain sample gets a placeholder entry, is queued for k_mlp_fix, and the
  * next sample is written unconditionally; k_mlp_dedupe then drops the repeats
  * around the resolved entries.  With exact != 0 every sample is binary64. */
-__global__ void __launch_bounds__(128, 4) k_mlp_fast(DevGeom g, int64_t n, const uint32_t* __restrict__ order,
+__global__ void __launch_bounds__(128, 5) k_mlp_fast(DevGeom g, int64_t n, const uint32_t* __restrict__ order,
                                                   HistView h, int bf16, float* __restrict__ chord,
                                                   float* __restrict__ row_scale,
                                                   const MlpRec* __restrict__ rec,

@@ -58,12 +58,19 @@ PCT_FN void pct_split(double a, double* hi, double* lo) {
     *hi = c - ab;
     *lo = a - *hi;
 }
+/* p = RN(a b) and its error e = a b - p exactly (both forms are exact away
+ * from overflow and underflow, so they give the same e: Dekker's product on
+ * the host, one fused multiply-add on the device). */
 PCT_FN void pct_two_prod(double a, double b, double* p, double* e) {
-    double ah, al, bh, bl;
     double x = a * b;
+#if defined(__CUDA_ARCH__)
+    *e = fma(a, b, -x);
+#else
+    double ah, al, bh, bl;
     pct_split(a, &ah, &al);
     pct_split(b, &bh, &bl);
     *e = ((ah * bh - x) + ah * bl + al * bh) + al * bl;
+#endif
     *p = x;
 }
 
@@ -153,6 +160,18 @@ PCT_FN double pct_cos(double x) {
         case 1: return -pct_sin_kernel(r, rr);
         case 2: return -pct_cos_kernel(r, rr);
         default: return pct_sin_kernel(r, rr);
+    }
+}
+/* pct_sin(x) and pct_cos(x) from one argument reduction (the same values). */
+PCT_FN void pct_sincos(double x, double* s, double* c) {
+    double r, rr;
+    int q = pct_rem_pio2(x, &r, &rr);
+    const double sk = pct_sin_kernel(r, rr), ck = pct_cos_kernel(r, rr);
+    switch (q) {
+        case 0: *s = sk; *c = ck; break;
+        case 1: *s = ck; *c = -sk; break;
+        case 2: *s = -sk; *c = -ck; break;
+        default: *s = -ck; *c = sk; break;
     }
 }
 /* tan = sin/cos from double-double kernel values, one exact-remainder correction. */
