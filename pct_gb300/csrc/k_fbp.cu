@@ -11,7 +11,7 @@
  *                  column and 16 slices, binary32 accumulation over angle bins
  *                  in order per voxel, per-angle cos/sin table in shared
  *                  memory, divisions from one reciprocal per column and angle
- *                  (div_rn); the sinogram (NUM_BINS floats) stays L2-resident
+ *                  (pct_div_rn); the sinogram (NUM_BINS floats) stays L2-resident
  *   k_fbp_hull     FBP_image_2_hull_GPU (.cu:3250)
  *   k_initial      define_initial_iterate (.cu:7191-7205)
  * Bound by binary64 throughput (each term of the reference is binary64).
@@ -72,24 +72,15 @@ __global__ void k_filter(int T, int A, double tb, const float* __restrict__ sino
     }
 }
 
-/* The correctly rounded quotient a / b from r = RN(1 / b): q = RN(a r), then
- * RN(q + (a - b q) r) with the remainder exact by FMA (Markstein's theorem:
- * r within half an ulp of 1 / b and q within one ulp of a / b give RN(a / b)).
- * Three binary64 instructions instead of a division; checked against IEEE
- * division on every quotient the backprojection forms for grids of 128x128x8
- * to 320x320x64 (3.5e9 quotients) and on 2e8 random operands, no difference. */
-__device__ __forceinline__ double div_rn(double a, double b, double r) {
-    const double q = a * r;
-    return fma(fma(-q, b, a), r, q);
-}
-
 /* One thread per voxel column (x, y) and group of BP_SLICES slices: the terms
  * of an angle that do not depend on z (u, t, the t bin, eta and the fan-beam
  * scale) are formed once per column and angle, the z terms per slice; each
  * slice keeps its own binary32 accumulator over the angle bins in order.
  * Every expression is the one of backprojection_GPU, its divisions by SR + u
- * and by the bin sizes formed by div_rn from one reciprocal per column and
- * angle, so the image is the same bit for bit. */
+ * and by the bin sizes formed by pct_div_rn from one reciprocal per column
+ * and angle (the same quotients: checked against IEEE division on every
+ * quotient of the parity and benchmark grids by tests/test_exact_arith.py),
+ * so the image is the same bit for bit. */
 constexpr int BP_SLICES = 16;
 __global__ void __launch_bounds__(128) k_backproject(DevGeom g, const float* __restrict__ sino,
                                                      const double2* __restrict__ trig, float* __restrict__ image) {
@@ -124,18 +115,18 @@ __global__ void __launch_bounds__(128) k_backproject(DevGeom g, const float* __r
         const double u = x * ca + y * sa;
         const double t = -x * sa + y * ca;
         const double d = SR + u, rd = 1.0 / d;
-        const double dnt = div_rn(t - u * div_rn(t, d, rd), tbs, r_tbs) + T / 2.0;
+        const double dnt = pct_div_rn(t - u * pct_div_rn(t, d, rd), tbs, r_tbs) + T / 2.0;
         int t_bin = pct_d2i(dnt);
         if (t_bin > dnt) t_bin -= 1;
         const double eta = dnt - t_bin;
-        const double sf = div_rn(SR, d, rd);
+        const double sf = pct_div_rn(SR, d, rd);
         const double scale = sf * sf;
         const int tbin_ab = t_bin + ab * T;
 #pragma unroll
         for (int k = 0; k < BP_SLICES; ++k) {
             if (k >= ns) break;
             const double v = z[k];
-            const double dnv = div_rn(v - u * div_rn(v, d, rd), vbs, r_vbs) + g.v_bins / 2.0;
+            const double dnv = pct_div_rn(v - u * pct_div_rn(v, d, rd), vbs, r_vbs) + g.v_bins / 2.0;
             int v_bin = pct_d2i(dnv);
             if (v_bin > dnv) v_bin -= 1;
             const double eps = dnv - v_bin;

@@ -2,7 +2,9 @@
  * Deterministic elementary functions for host C/C++ and CUDA device code.
  *
  * Every function here is written with IEEE-754 binary64 add, subtract,
- * multiply, divide, sqrt and floor only, evaluated in source order.  Built
+ * multiply, divide, sqrt, floor and fused multiply-add only, evaluated in
+ * source order (the fused multiply-adds where they are exact or correctly
+ * rounded by construction: pct_two_prod on the device, pct_div_rn).  Built
  * without FMA contraction (gcc -ffp-contract=off, nvcc -fmad=false) the same
  * source gives bit-identical results on x86-64, aarch64 and sm_103a, which is
  * what lets the CUDA kernels and the CPU oracle agree bit for bit on the
@@ -72,6 +74,16 @@ PCT_FN void pct_two_prod(double a, double b, double* p, double* e) {
     *e = ((ah * bh - x) + ah * bl + al * bh) + al * bl;
 #endif
     *p = x;
+}
+
+/* The correctly rounded quotient a / b from r = RN(1 / b): q = RN(a r), then
+ * RN(q + (a - b q) r) with the remainder a - b q exact by FMA.  Markstein's
+ * theorem: with r within half an ulp of 1 / b and q within one ulp of a / b,
+ * the corrected q is RN(a / b) (no overflow or underflow).  Three binary64
+ * instructions where the divisor is reused with its reciprocal. */
+PCT_FN double pct_div_rn(double a, double b, double r) {
+    const double q = a * r;
+    return fma(fma(-q, b, a), r, q);
 }
 
 /* x^2 correctly rounded is just x*x; x^3 with a single rounding. */
