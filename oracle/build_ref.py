@@ -52,6 +52,16 @@ GEOMETRIES = {
         "GANTRY_ANGLE_INTERVAL": "4.0",
         "ANGULAR_BIN_SIZE": "4.0",
     },
+    # Smallest grid of the batched-scan family: 128x128x8 at 1x1x2.5 mm,
+    # r = 6.4 cm, 2 degree steps (180 angles).
+    "cfg3_128x8": {
+        "RECON_CYL_RADIUS": "6.4",
+        "COLUMNS": "128",
+        "ROWS": "128",
+        "SSD_V_SIZE": "3.0",
+        "GANTRY_ANGLE_INTERVAL": "2.0",
+        "ANGULAR_BIN_SIZE": "2.0",
+    },
 }
 
 REF_TU = os.path.join("src", "pCT_Reconstruction_Data_Segments.cu")

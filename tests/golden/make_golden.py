@@ -45,6 +45,11 @@ def scenarios():
         # 200x200x8 water-cylinder geometry with the SM hull
         "cfg1_sm": dict(geometry="cfg1", workload=phantoms.cfg1(num_histories=120000, seed=5),
                         run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=0), mlp_rows=1500),
+        # ellipsoid phantom of the batched-scan family on its smallest grid, 180 angles, through DROP
+        "cfg3_128x8": dict(geometry="cfg3_128x8",
+                           workload=phantoms.ellipsoids(31, num_histories=150000, cols=128, slices=8),
+                           run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=2, block_size=50000, lambda_=0.1),
+                           mlp_rows=1500),
     }
 
 
@@ -57,7 +62,9 @@ def pack(name, arr, out):
     out["dtype:" + name] = np.array(str(arr.dtype))
     out["shape:" + name] = np.array(arr.shape, dtype=np.int64)
     out["sha:" + name] = np.array(digest(arr))
-    if arr.size <= FULL_LIMIT:
+    # DROP iterates in full whatever their size: they are compared within a
+    # tolerance, not by digest
+    if arr.size <= FULL_LIMIT or (name.startswith("x_") and name[2:].isdigit()):
         out["full:" + name] = arr
     else:
         out["head:" + name] = arr.ravel()[:SAMPLE]
@@ -97,6 +104,8 @@ def make(name, sc, ref_root):
     out = {"scenario": np.array(name), "workload": np.array(w.name), "seed": np.array(w.seed),
            "num_histories": np.array(w.num_histories), "v_extent": np.array(w.v_extent),
            "input_sha": np.array(digest(data) + digest(angles)),
+           "grid_cols": np.array(int(w.config["columns"])),
+           "grid_slices": np.array(int(round((w.config["ssd_v_size"] - 1.0) / 0.25))),
            "run_config": np.array(repr(sc["run"]))}
     for k, v in res.items():
         if k.startswith("__"):

@@ -29,6 +29,9 @@ def load_fixture(path):
 
 
 def workload_of(fx):
+    if str(fx["workload"]).startswith("ellipsoids_"):
+        return phantoms.ellipsoids(int(fx["seed"]), num_histories=int(fx["num_histories"]),
+                                   cols=int(fx["grid_cols"]), slices=int(fx["grid_slices"]))
     kw = dict(num_histories=int(fx["num_histories"]), seed=int(fx["seed"]))
     if str(fx["workload"]) == "tiny":
         kw["v_extent"] = float(fx["v_extent"])
