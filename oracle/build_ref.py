@@ -52,6 +52,16 @@ GEOMETRIES = {
         "GANTRY_ANGLE_INTERVAL": "4.0",
         "ANGULAR_BIN_SIZE": "4.0",
     },
+    # The benchmark scan's grid: 256x256x32 at 1x1x2.5 mm, r = 12.8 cm,
+    # 2 degree steps (180 angles).
+    "cfg2": {
+        "RECON_CYL_RADIUS": "12.8",
+        "COLUMNS": "256",
+        "ROWS": "256",
+        "SSD_V_SIZE": "9.0",
+        "GANTRY_ANGLE_INTERVAL": "2.0",
+        "ANGULAR_BIN_SIZE": "2.0",
+    },
     # Smallest grid of the batched-scan family: 128x128x8 at 1x1x2.5 mm,
     # r = 6.4 cm, 2 degree steps (180 angles).
     "cfg3_128x8": {

@@ -19,7 +19,7 @@ from oracle import oracle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
-WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1}
+WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1, "cfg2": phantoms.cfg2}
 DROP_TOL = 1e-6
 
 
