@@ -7,6 +7,7 @@ fixture run added them) and must reproduce every stage bit for bit; the DROP
 iterates, which the reference keeps in binary32, must match the oracle's
 binary64 run within 1e-6 relative L2.
 """
+import ast
 import glob
 import hashlib
 import os
@@ -39,7 +40,7 @@ def workload_of(fx):
 
 
 def run_kwargs(fx):
-    return eval(str(fx["run_config"]), {"__builtins__": {}})
+    return ast.literal_eval(str(fx["run_config"]))
 
 
 def names(fx):
