@@ -77,7 +77,8 @@ class Clocks:
     """nvidia-smi sampler running during the timed region."""
 
     def __init__(self, gpu):
-        self.path = tempfile.mktemp(suffix=".csv")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        self.f = os.fdopen(fd, "w")
         self.gpu = gpu
         self.p = None
 
@@ -86,10 +87,9 @@ class Clocks:
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
-            self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q, "--format=csv,noheader",
                                        "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
-        except Exception:
+        except OSError:  # no nvidia-smi: the line reports no clock samples
             self.p = None
         return self
 
@@ -97,7 +97,7 @@ class Clocks:
         if self.p:
             self.p.terminate()
             self.p.wait()
-            self.f.close()
+        self.f.close()
 
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
@@ -116,6 +116,11 @@ class Clocks:
                         reasons.add(name)
         except OSError:
             pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None, "reasons": sorted(reasons),
                 "samples": len(sm)}
 
