@@ -190,7 +190,7 @@ def run_reference_arm(a, ws, rank):
     data, angles = phantoms.generate(w)
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    ora = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_EXACT, iterations=0, keep_history=True)
+    ora = oracle.run_pipeline(cfg, data, angles, iterations=0, keep_history=True)
     hr = ora["_hr"]
     sample = min(len(hr["WEPL"]), 40000)
     h = {k: v[:sample].copy() for k, v in hr.items()}

@@ -19,7 +19,6 @@ if ROOT not in sys.path:
 from pct_gb300 import _capi  # noqa: E402
 from oracle import build_oracle  # noqa: E402
 
-SUM_EXACT, SUM_SEQUENTIAL = 0, 1
 _lib = None
 
 
@@ -81,7 +80,7 @@ def preprocess(cfg, data13, proj_angle):
     return out
 
 
-def bin_statistics(cfg, h, sum_mode):
+def bin_statistics(cfg, h):
     lib = load()
     g = geometry(cfg)
     nb = g.num_bins
@@ -90,13 +89,13 @@ def bin_statistics(cfg, h, sum_mode):
     n = len(h["bin_num"])
     rc = lib.ora_bin_statistics(_cfgp(cfg), C.c_int64(n), _p(h["bin_num"]), _p(h["bin_valid"]), _p(h["WEPL"]),
                                 _p(h["xy_entry_angle"]), _p(h["xz_entry_angle"]), _p(h["xy_exit_angle"]),
-                                _p(h["xz_exit_angle"]), sum_mode, _p(r["counts"]), _p(r["mean_WEPL"]),
+                                _p(h["xz_exit_angle"]), _p(r["counts"]), _p(r["mean_WEPL"]),
                                 _p(r["mean_ut"]), _p(r["mean_uv"]), _p(r["sd_WEPL"]), _p(r["sd_ut"]), _p(r["sd_uv"]))
     assert rc == 0
     return r
 
 
-def statistical_cuts(cfg, h, st, sum_mode):
+def statistical_cuts(cfg, h, st):
     lib = load()
     g = geometry(cfg)
     n = len(h["bin_num"])
@@ -106,7 +105,7 @@ def statistical_cuts(cfg, h, st, sum_mode):
     rc = lib.ora_statistical_cuts(_cfgp(cfg), C.c_int64(n), _p(h["bin_num"]), _p(h["WEPL"]), _p(h["xy_entry_angle"]),
                                   _p(h["xz_entry_angle"]), _p(h["xy_exit_angle"]), _p(h["xz_exit_angle"]),
                                   _p(st["mean_WEPL"]), _p(st["mean_ut"]), _p(st["mean_uv"]), _p(st["sd_WEPL"]),
-                                  _p(st["sd_ut"]), _p(st["sd_uv"]), sum_mode, _p(failed), _p(counts), _p(sino))
+                                  _p(st["sd_ut"]), _p(st["sd_uv"]), _p(failed), _p(counts), _p(sino))
     assert rc == 0
     return failed, counts, sino
 
@@ -235,7 +234,7 @@ def _select(h, mask):
     return {k: v[mask] for k, v in h.items() if isinstance(v, np.ndarray) and v.ndim == 1 and len(v) == len(mask)}
 
 
-def run_pipeline(cfg, data13, proj_angle, sum_mode=SUM_EXACT, iterations=None, block_size=None, lam=None,
+def run_pipeline(cfg, data13, proj_angle, iterations=None, block_size=None, lam=None,
                  keep_history=False):
     """The reference's main() sequence on the oracle.  Returns named stage outputs."""
     out = {}
@@ -261,11 +260,11 @@ def run_pipeline(cfg, data13, proj_angle, sum_mode=SUM_EXACT, iterations=None, b
         out["SM_counts_h"] = sm
         out["x_SM"], out["sm_thresholds"] = sm_edge(cfg, sm)
         out["sm_walk_stats"] = st
-    st = bin_statistics(cfg, hk, sum_mode)
+    st = bin_statistics(cfg, hk)
     out["bin_counts_h_pre"] = st["counts"]
     out["mean_WEPL_h"], out["mean_rel_ut_angle_h"], out["mean_rel_uv_angle_h"] = st["mean_WEPL"], st["mean_ut"], st["mean_uv"]
     out["stddev_WEPL_h"], out["stddev_rel_ut_angle_h"], out["stddev_rel_uv_angle_h"] = st["sd_WEPL"], st["sd_ut"], st["sd_uv"]
-    failed, counts_post, sino = statistical_cuts(cfg, hk, st, sum_mode)
+    failed, counts_post, sino = statistical_cuts(cfg, hk, st)
     out["failed_cuts"] = failed
     passed = failed == 0
     hc = _select(hk, passed)

@@ -189,18 +189,6 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
 /* ------------------------------------------------------------------------- */
 /* a4-a6: bin statistics, cuts, sinogram                                      */
 /* ------------------------------------------------------------------------- */
-/* Fixed-point scales of the exact sums (values are binary32, so these are
- * exact for every summand of magnitude >= 2^(24 - scale)). */
-#define SCALE_WEPL 4294967296.0           /* 2^32 */
-#define SCALE_ANGLE 1099511627776.0       /* 2^40 */
-#define SCALE_ANGLE_SQ 281474976710656.0  /* 2^48 */
-
-static int64_t to_fixed(float v, double scale) {
-    double s = (double)v * scale;
-    return (int64_t)(s >= 0 ? s + 0.5 : s - 0.5);
-}
-static float from_fixed(int64_t s, double scale) { return (float)((double)s / scale); }
-
 /* relative angle with the +-2 pi wrap (.cu:2557-2566, 2681-2690, 2847-2856) */
 static double rel_angle(float exit_angle, float entry_angle) {
     double r = exit_angle - entry_angle;
@@ -211,41 +199,29 @@ static double rel_angle(float exit_angle, float entry_angle) {
 
 int ora_bin_statistics(const pct_config* cfg, int64_t n, const int32_t* bin_num, const uint8_t* bin_valid,
                        const float* wepl, const float* xy_entry_angle, const float* xz_entry_angle,
-                       const float* xy_exit_angle, const float* xz_exit_angle, int sum_mode,
+                       const float* xy_exit_angle, const float* xz_exit_angle,
                        int32_t* counts, float* mean_wepl, float* mean_ut, float* mean_uv,
                        float* sd_wepl, float* sd_ut, float* sd_uv) {
     pct_geometry g;
     if (pct_geometry_derive(cfg, &g)) return 1;
     const int nb = g.num_bins;
     memset(counts, 0, sizeof(int32_t) * nb);
-    int64_t* s1 = (int64_t*)calloc((size_t)nb * 3, sizeof(int64_t));
-    int64_t* s2 = (int64_t*)calloc((size_t)nb * 3, sizeof(int64_t));
-    if (!s1 || !s2) { free(s1); free(s2); return 2; }
     for (int b = 0; b < nb; ++b) mean_wepl[b] = mean_ut[b] = mean_uv[b] = sd_wepl[b] = sd_ut[b] = sd_uv[b] = 0.0f;
-    /* binning_GPU sums (.cu:2557-2570): only histories with a valid bin */
+    /* binning_GPU sums (.cu:2557-2570): only histories with a valid bin.  Every
+     * sum here is binary32, added left to right in history order: the order of
+     * the reference's atomicAdd calls in a sequential run of its kernels. */
     for (int64_t i = 0; i < n; ++i) {
         if (!bin_valid[i]) continue;
         int b = bin_num[i];
         float rut = (float)rel_angle(xy_exit_angle[i], xy_entry_angle[i]);
         float ruv = (float)rel_angle(xz_exit_angle[i], xz_entry_angle[i]);
         counts[b] += 1;
-        if (sum_mode == ORA_SUM_SEQUENTIAL) {
-            mean_wepl[b] = mean_wepl[b] + wepl[i];
-            mean_ut[b] = mean_ut[b] + rut;
-            mean_uv[b] = mean_uv[b] + ruv;
-        } else {
-            s1[3 * b + 0] += to_fixed(wepl[i], SCALE_WEPL);
-            s1[3 * b + 1] += to_fixed(rut, SCALE_ANGLE);
-            s1[3 * b + 2] += to_fixed(ruv, SCALE_ANGLE);
-        }
+        mean_wepl[b] = mean_wepl[b] + wepl[i];
+        mean_ut[b] = mean_ut[b] + rut;
+        mean_uv[b] = mean_uv[b] + ruv;
     }
     /* calculate_means_GPU (.cu:2618-2627) */
     for (int b = 0; b < nb; ++b) {
-        if (sum_mode != ORA_SUM_SEQUENTIAL) {
-            mean_wepl[b] = from_fixed(s1[3 * b + 0], SCALE_WEPL);
-            mean_ut[b] = from_fixed(s1[3 * b + 1], SCALE_ANGLE);
-            mean_uv[b] = from_fixed(s1[3 * b + 2], SCALE_ANGLE);
-        }
         if (counts[b] > 0) {
             mean_wepl[b] /= counts[b];
             mean_ut[b] /= counts[b];
@@ -261,23 +237,12 @@ int ora_bin_statistics(const pct_config* cfg, int64_t n, const int32_t* bin_num,
         double dut = rut - mean_ut[b];
         double duv = ruv - mean_uv[b];
         float qw = (float)(dw * dw), qut = (float)(dut * dut), quv = (float)(duv * duv);
-        if (sum_mode == ORA_SUM_SEQUENTIAL) {
-            sd_wepl[b] = sd_wepl[b] + qw;
-            sd_ut[b] = sd_ut[b] + qut;
-            sd_uv[b] = sd_uv[b] + quv;
-        } else {
-            s2[3 * b + 0] += to_fixed(qw, SCALE_WEPL);
-            s2[3 * b + 1] += to_fixed(qut, SCALE_ANGLE_SQ);
-            s2[3 * b + 2] += to_fixed(quv, SCALE_ANGLE_SQ);
-        }
+        sd_wepl[b] = sd_wepl[b] + qw;
+        sd_ut[b] = sd_ut[b] + qut;
+        sd_uv[b] = sd_uv[b] + quv;
     }
     /* calculate_standard_deviations_GPU (.cu:2718-2730) */
     for (int b = 0; b < nb; ++b) {
-        if (sum_mode != ORA_SUM_SEQUENTIAL) {
-            sd_wepl[b] = from_fixed(s2[3 * b + 0], SCALE_WEPL);
-            sd_ut[b] = from_fixed(s2[3 * b + 1], SCALE_ANGLE_SQ);
-            sd_uv[b] = from_fixed(s2[3 * b + 2], SCALE_ANGLE_SQ);
-        }
         if (counts[b] > 1) {
             int div = counts[b] - (cfg->sample_std_dev ? 1 : 0);
             sd_wepl[b] = sqrtf(sd_wepl[b] / div);
@@ -285,8 +250,6 @@ int ora_bin_statistics(const pct_config* cfg, int64_t n, const int32_t* bin_num,
             sd_uv[b] = sqrtf(sd_uv[b] / div);
         }
     }
-    free(s1);
-    free(s2);
     return 0;
 }
 
@@ -294,13 +257,11 @@ int ora_statistical_cuts(const pct_config* cfg, int64_t n, const int32_t* bin_nu
                          const float* xy_entry_angle, const float* xz_entry_angle, const float* xy_exit_angle,
                          const float* xz_exit_angle, const float* mean_wepl, const float* mean_ut,
                          const float* mean_uv, const float* sd_wepl, const float* sd_ut, const float* sd_uv,
-                         int sum_mode, uint8_t* failed, int32_t* counts_post, float* sinogram) {
+                         uint8_t* failed, int32_t* counts_post, float* sinogram) {
     pct_geometry g;
     if (pct_geometry_derive(cfg, &g)) return 1;
     const int nb = g.num_bins;
     const int K = cfg->sigmas_to_keep;
-    int64_t* s = (int64_t*)calloc((size_t)nb, sizeof(int64_t));
-    if (!s) return 2;
     memset(counts_post, 0, sizeof(int32_t) * nb);
     for (int b = 0; b < nb; ++b) sinogram[b] = 0.0f;
     /* statistical_cuts_GPU (.cu:2844-2868) */
@@ -315,16 +276,12 @@ int ora_statistical_cuts(const pct_config* cfg, int64_t n, const int32_t* bin_nu
         failed[i] = (uint8_t)f;
         if (!f) {
             counts_post[b] += 1;
-            if (sum_mode == ORA_SUM_SEQUENTIAL) sinogram[b] = sinogram[b] + wepl[i];
-            else s[b] += to_fixed(wepl[i], SCALE_WEPL);
+            sinogram[b] = sinogram[b] + wepl[i]; /* binary32, history order */
         }
     }
     /* construct_sinogram_GPU (.cu:2912-2917) */
-    for (int b = 0; b < nb; ++b) {
-        if (sum_mode != ORA_SUM_SEQUENTIAL) sinogram[b] = from_fixed(s[b], SCALE_WEPL);
+    for (int b = 0; b < nb; ++b)
         if (counts_post[b] > 0) sinogram[b] /= counts_post[b];
-    }
-    free(s);
     return 0;
 }
 

@@ -14,10 +14,9 @@
  *
  * Arithmetic: binary64/binary32 operations in the reference's source order,
  * no FMA contraction (built with -ffp-contract=off), elementary functions
- * from pct_gb300/csrc/pct_math.h.  Two summation modes for the per-bin
- * statistics: ORA_SUM_EXACT (exact fixed-point sums, the product's
- * definition) and ORA_SUM_SEQUENTIAL (binary32 sums in history order, the
- * order in which the sequential reference harness adds).
+ * from pct_gb300/csrc/pct_math.h.  The per-bin statistics and the sinogram
+ * are binary32 sums in history order: the order in which a sequential run of
+ * the reference's atomicAdd kernels adds them (the golden fixtures' run).
  */
 #ifndef PCT_ORACLE_H
 #define PCT_ORACLE_H
@@ -29,8 +28,6 @@
 extern "C" {
 #endif
 
-enum { ORA_SUM_EXACT = 0, ORA_SUM_SEQUENTIAL = 1 };
-
 /* a1-a3: unit conversion, cylinder intersections, bin index; per history. */
 int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13], const float* projection_angle,
                    int32_t* gantry_angle, uint8_t* missed, int32_t* bin_num, uint8_t* bin_valid,
@@ -41,7 +38,7 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
 /* a4: per-bin counts, means and standard deviations over the kept histories. */
 int ora_bin_statistics(const pct_config* cfg, int64_t n, const int32_t* bin_num, const uint8_t* bin_valid,
                        const float* wepl, const float* xy_entry_angle, const float* xz_entry_angle,
-                       const float* xy_exit_angle, const float* xz_exit_angle, int sum_mode,
+                       const float* xy_exit_angle, const float* xz_exit_angle,
                        int32_t* counts, float* mean_wepl, float* mean_ut, float* mean_uv,
                        float* sd_wepl, float* sd_ut, float* sd_uv);
 
@@ -50,7 +47,7 @@ int ora_statistical_cuts(const pct_config* cfg, int64_t n, const int32_t* bin_nu
                          const float* xy_entry_angle, const float* xz_entry_angle, const float* xy_exit_angle,
                          const float* xz_exit_angle, const float* mean_wepl, const float* mean_ut,
                          const float* mean_uv, const float* sd_wepl, const float* sd_ut, const float* sd_uv,
-                         int sum_mode, uint8_t* failed, int32_t* counts_post, float* sinogram);
+                         uint8_t* failed, int32_t* counts_post, float* sinogram);
 
 /* a7: hull walks.  kind 0 SC (hull 0/1 image), 1 MSC, 2 SM (count images).
  * The image must be initialised with ora_initialize_hull() first. */

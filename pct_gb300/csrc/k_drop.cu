@@ -6,20 +6,20 @@
  * (.cu:5774-5841) without the MLP: the dot of every row with the iterate at
  * the start of the block, the update value c * lambda * (b - c sum x) / ||a||^2
  * (binary32, with 1 / (c |a|) rounded once from binary64), its addition to every
- * voxel of the row, and the squared residual (summed in binary64 per CTA); a
- * second launch is image_update_GPU
+ * voxel of the row, and the squared residual (each row's square and every sum
+ * of them in binary64); a second launch is image_update_GPU
  * (.cu:5900-5938): x += x_update / s_j with s_j the number of block row
  * entries in voxel j (the DROP diagonal weight).  s_j depends only on the
  * rows and the block split, so it is counted once per set of rows instead of
  * in every iteration.  One CUDA graph holds the 2 * blocks launches of an
  * iteration.
  *
- * Forms: the tiled form (k_drop_tiled.cu, default where it fits) regroups
- * the rows by image tile; the scatter form runs one warp per row in history
+ * Forms: the scatter form (the default) runs one warp per row in history
  * order with one L2 reduction per row entry (k_drop_rows + k_drop_relax), the
  * direct transcription of the block update; the sorted form is the scatter
  * form visiting each block's rows in sinogram bin order (a per-block
- * counting sort, once per set of rows).
+ * counting sort, once per set of rows); the tiled form (k_drop_tiled.cu)
+ * regroups the rows by image tile and sums in fixed point (reproducible).
  */
 #include <cstring>
 #include "pct_device.cuh"
@@ -62,10 +62,15 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
                                                             const float* __restrict__ x, float* __restrict__ upd,
                                                             uint32_t nv, double* __restrict__ resid, float eta,
                                                             float psi_sign) {
-    __shared__ float sres[DROP_WARPS];
+    __shared__ double sres[DROP_WARPS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t stride = (int64_t)gridDim.x * DROP_WARPS;
-    float r2 = 0.0f; /* lane 0: this warp's rows */
+    /* The squared residuals in binary64: lane (k mod 32) keeps the residual of
+     * the warp's k-th row until 32 rows are pending, then every lane adds its
+     * exact square with one FMA (one binary64 warp instruction per 32 rows). */
+    double r2 = 0.0;
+    float pend = 0.0f;
+    int nrow = 0;
     /* persistent warps: one row at a time, its first 32 * DROP_REG entries held in
      * registers between the dot and the update (independent loads, one read of the row) */
     for (int64_t j = start + (int64_t)blockIdx.x * DROP_WARPS + w; j < end; j += stride) {
@@ -112,14 +117,20 @@ __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64
                 if (v < nv) atomicAdd(upd + v, value);
             }
         }
-        r2 += res * res;
+        if (lane == (nrow & 31)) pend = res;
+        if ((++nrow & 31) == 0) {
+            r2 = fma((double)pend, (double)pend, r2);
+            pend = 0.0f;
+        }
     }
+    r2 = fma((double)pend, (double)pend, r2);
+    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
     if (lane == 0) sres[w] = r2;
     __syncthreads();
     if (threadIdx.x == 0) {
-        float s = 0.0f;
+        double s = 0.0;
         for (int k = 0; k < DROP_WARPS; ++k) s += sres[k];
-        if (s != 0.0f) atomicAdd(resid, (double)s); /* the iteration's sum in binary64 */
+        if (s != 0.0) atomicAdd(resid, s);
     }
 }
 
@@ -192,30 +203,6 @@ __global__ void k_sort_count(int64_t start, int64_t end, const int32_t* __restri
     atomicAdd(cnt + (key < nkeys ? key : 0u), 1u);
 }
 
-__device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_t* ws, uint32_t* total) {
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) ws[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        uint32_t s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0u;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        ws[lane] = s;
-    }
-    __syncthreads();
-    uint32_t r = x - v + (w > 0 ? ws[w - 1] : 0u);
-    *total = ws[(blockDim.x >> 5) - 1];
-    __syncthreads();
-    return r;
-}
-
 /* tile sums of the counts (one CTA per 4096 keys) */
 __global__ void __launch_bounds__(1024) k_scan_tile_sum_u32(const uint32_t* __restrict__ cnt, uint32_t nkeys,
                                                             uint32_t* __restrict__ tsum) {
@@ -223,7 +210,7 @@ __global__ void __launch_bounds__(1024) k_scan_tile_sum_u32(const uint32_t* __re
     uint32_t k0 = blockIdx.x * SCAN_TILE + threadIdx.x * 4, s = 0;
     for (int k = 0; k < 4; ++k) s += k0 + k < nkeys ? cnt[k0 + k] : 0u;
     uint32_t total;
-    block_exclusive_scan_u32(s, ws, &total);
+    dev_block_exclusive_scan_u32(s, ws, &total);
     if (threadIdx.x == 0) tsum[blockIdx.x] = total;
 }
 
@@ -234,7 +221,7 @@ __global__ void __launch_bounds__(1024) k_scan_tiles_u32(uint32_t* __restrict__ 
     for (int base = 0; base < tiles; base += 1024) {
         int k = base + threadIdx.x;
         uint32_t v = k < tiles ? tsum[k] : 0u, total;
-        uint32_t ex = block_exclusive_scan_u32(v, ws, &total);
+        uint32_t ex = dev_block_exclusive_scan_u32(v, ws, &total);
         if (k < tiles) tsum[k] = carry + ex;
         carry += total;
     }
@@ -252,7 +239,7 @@ __global__ void __launch_bounds__(1024) k_scan_apply_u32(const uint32_t* __restr
         s += e[k];
     }
     uint32_t total;
-    uint32_t run = block_exclusive_scan_u32(s, ws, &total) + tsum[blockIdx.x];
+    uint32_t run = dev_block_exclusive_scan_u32(s, ws, &total) + tsum[blockIdx.x];
     for (int k = 0; k < 4; ++k) {
         if (k0 + k < nkeys) off[k0 + k] = run;
         run += e[k];

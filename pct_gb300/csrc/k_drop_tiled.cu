@@ -250,11 +250,11 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_tile_rows(int64_t start, int64
                                                             const float* __restrict__ wepl, float lambda,
                                                             float* __restrict__ u, unsigned* __restrict__ umax,
                                                             double* __restrict__ resid) {
-    __shared__ float sres[ROWS_THREADS / 32];
+    __shared__ double sres[ROWS_THREADS / 32];
     __shared__ unsigned smax[ROWS_THREADS / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t i = start + (int64_t)blockIdx.x * ROWS_THREADS + threadIdx.x;
-    float r2 = 0.0f;
+    double r2 = 0.0; /* the squared residual and its sums in binary64 */
     unsigned mx = 0;
     if (i < end) {
         long long sum = 0;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_tile_rows(int64_t start, int64
         const float res = fmaf(-c, dot, wepl[i]);
         const float val = (res * row_scale[i]) * lambda;
         u[i - start] = val;
-        r2 = res * res;
+        r2 = (double)res * (double)res; /* exact */
         mx = __float_as_uint(fabsf(val)); /* non-negative floats order like their bits; NaN sorts above inf */
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -278,13 +278,13 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_tile_rows(int64_t start, int64
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float s = 0.0f;
+        double s = 0.0;
         unsigned m = 0;
         for (int k = 0; k < ROWS_THREADS / 32; ++k) {
             s += sres[k];
             m = smax[k] > m ? smax[k] : m;
         }
-        if (s != 0.0f) atomicAdd(resid, (double)s);
+        if (s != 0.0) atomicAdd(resid, s);
         if (m) atomicMax(umax, m);
     }
 }

@@ -58,10 +58,10 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_rows(int64_t start, int64_t e
                                                         const float* __restrict__ wepl, float lambda,
                                                         const float* __restrict__ x, float* __restrict__ upd,
                                                         uint32_t nv, double* __restrict__ resid) {
-    __shared__ float sres[NA_WARPS];
+    __shared__ double sres[NA_WARPS];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t i = start + (int64_t)blockIdx.x * NA_WARPS + w;
-    float r2 = 0.0f;
+    double r2 = 0.0; /* the squared residual and its sums in binary64 */
     if (i < end) {
         int64_t a = off[i], b = off[i + 1];
         float dot = 0.0f;
@@ -77,14 +77,14 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_rows(int64_t start, int64_t e
             uint32_t v = rows[p];
             if (v < nv) atomicAdd(upd + v, value);
         }
-        r2 = res * res;
+        r2 = (double)res * (double)res; /* exact */
     }
     if (lane == 0) sres[w] = r2;
     __syncthreads();
     if (threadIdx.x == 0 && resid) {
-        float s = 0.0f;
+        double s = 0.0;
         for (int k = 0; k < NA_WARPS; ++k) s += sres[k];
-        if (s != 0.0f) atomicAdd(resid, (double)s);
+        if (s != 0.0) atomicAdd(resid, s);
     }
 }
 

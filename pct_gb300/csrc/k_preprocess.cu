@@ -1,19 +1,15 @@
 /*
- * Stages a1-a6 of the path: unit conversion, reconstruction-cylinder
- * intersections, binning, per-bin statistics, 3-sigma cuts and the sinogram.
+ * Stages a1-a3 of the path: unit conversion, reconstruction-cylinder
+ * intersections and binning, per chunk of histories.
  *
- *   k_preprocess    one thread per history, fused a1+a2+a3 and the first
- *                   statistics pass (read_data_chunk_v02 conversion .cu:1883-1921,
- *                   recon_volume_intersections_GPU .cu:2169-2387, binning_GPU
- *                   .cu:2507-2578).  SoA in, SoA out; per-bin sums go to exact
- *                   int64 fixed-point accumulators (order independent), where the
- *                   reference adds binary32 atomics in arbitrary order.
- *   k_means, k_sq_dev, k_sigma   calculate_means_GPU, sum_squared_deviations_GPU,
- *                   calculate_standard_deviations_GPU (.cu:2618-2730)
- *   k_cuts, k_sinogram           statistical_cuts_GPU, construct_sinogram_GPU
- *                   (.cu:2835-2917)
- * HBM-bound streaming kernels except k_preprocess, which is bound by binary64
- * arithmetic (a few hundred flops per history on a part with little FP64).
+ *   k_preprocess    one thread per history, fused a1+a2+a3 (read_data_chunk_v02
+ *                   conversion .cu:1883-1921, recon_volume_intersections_GPU
+ *                   .cu:2169-2387, binning_GPU .cu:2507-2578).  SoA in, SoA out;
+ *                   the bin counts are integer atomics.  The per-bin sums of
+ *                   binning_GPU (.cu:2567-2570) are formed later, in history
+ *                   order, with the other statistics (k_binstats.cu).
+ * k_preprocess is bound by binary64 arithmetic (a few hundred flops per
+ * history on a part with little FP64).
  */
 #include "pct_device.cuh"
 
@@ -75,8 +71,7 @@ __global__ void k_trig_table(double2* __restrict__ out, int n, double a, double 
 __global__ void __launch_bounds__(256) k_preprocess(DevGeom g, In13 in, const float* __restrict__ proj, int64_t n,
                                                     const double2* __restrict__ trig_gantry,
                                                     const double2* __restrict__ trig_bins, HistView out,
-                                                    uint8_t* __restrict__ missed, int* __restrict__ counts,
-                                                    long long* __restrict__ sum1, int angular_bin_deg_div) {
+                                                    uint8_t* __restrict__ missed, int* __restrict__ counts) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     /* a1 (.cu:1883-1897, 1921) */
@@ -168,106 +163,8 @@ __global__ void __launch_bounds__(256) k_preprocess(DevGeom g, In13 in, const fl
     out.failed[i] = 0;
     out.first_voxel[i] = 0;
     missed[i] = m;
-    /* binning sums (.cu:2551-2570) */
-    if (!m && valid) {
-        float rut = (float)dev_rel_angle(xy_out, xy_in);
-        float ruv = (float)dev_rel_angle(xz_out, xz_in);
-        atomicAdd(counts + bin, 1);
-        dev_add_fixed(sum1 + 3 * (int64_t)bin + 0, dev_to_fixed(w, PCT_SCALE_WEPL));
-        dev_add_fixed(sum1 + 3 * (int64_t)bin + 1, dev_to_fixed(rut, PCT_SCALE_ANGLE));
-        dev_add_fixed(sum1 + 3 * (int64_t)bin + 2, dev_to_fixed(ruv, PCT_SCALE_ANGLE));
-    }
-}
-
-/* calculate_means_GPU (.cu:2618-2627) on the exact sums */
-__global__ void k_means(int nb, const int* __restrict__ counts, const long long* __restrict__ sum1,
-                        float* __restrict__ mw, float* __restrict__ mut, float* __restrict__ muv) {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    float a = dev_from_fixed(sum1[3 * (int64_t)b + 0], PCT_SCALE_WEPL);
-    float u = dev_from_fixed(sum1[3 * (int64_t)b + 1], PCT_SCALE_ANGLE);
-    float v = dev_from_fixed(sum1[3 * (int64_t)b + 2], PCT_SCALE_ANGLE);
-    int c = counts[b];
-    if (c > 0) {
-        a /= c;
-        u /= c;
-        v /= c;
-    }
-    mw[b] = a;
-    mut[b] = u;
-    muv[b] = v;
-}
-
-/* sum_squared_deviations_GPU (.cu:2678-2698): every kept history, bin 0 included */
-__global__ void __launch_bounds__(256) k_sq_dev(int64_t n, HistView h, const float* __restrict__ mw,
-                                                const float* __restrict__ mut, const float* __restrict__ muv,
-                                                long long* __restrict__ sum2) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int b = h.bin_num[i];
-    double rut = dev_rel_angle(h.xy_exit_angle[i], h.xy_entry_angle[i]);
-    double ruv = dev_rel_angle(h.xz_exit_angle[i], h.xz_entry_angle[i]);
-    double dw = h.wepl[i] - mw[b];
-    double dut = rut - mut[b];
-    double duv = ruv - muv[b];
-    dev_add_fixed(sum2 + 3 * (int64_t)b + 0, dev_to_fixed((float)(dw * dw), PCT_SCALE_WEPL));
-    dev_add_fixed(sum2 + 3 * (int64_t)b + 1, dev_to_fixed((float)(dut * dut), PCT_SCALE_ANGLE_SQ));
-    dev_add_fixed(sum2 + 3 * (int64_t)b + 2, dev_to_fixed((float)(duv * duv), PCT_SCALE_ANGLE_SQ));
-}
-
-/* calculate_standard_deviations_GPU (.cu:2718-2730); also clears the counts
- * for the post-cut recount like the reference (.cu:2730). */
-__global__ void k_sigma(int nb, const int* __restrict__ counts, const long long* __restrict__ sum2, int sample,
-                        float* __restrict__ sw, float* __restrict__ sut, float* __restrict__ suv) {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    float a = dev_from_fixed(sum2[3 * (int64_t)b + 0], PCT_SCALE_WEPL);
-    float u = dev_from_fixed(sum2[3 * (int64_t)b + 1], PCT_SCALE_ANGLE_SQ);
-    float v = dev_from_fixed(sum2[3 * (int64_t)b + 2], PCT_SCALE_ANGLE_SQ);
-    int c = counts[b];
-    if (c > 1) {
-        int div = c - sample;
-        a = sqrtf(a / div);
-        u = sqrtf(u / div);
-        v = sqrtf(v / div);
-    }
-    sw[b] = a;
-    sut[b] = u;
-    suv[b] = v;
-}
-
-/* statistical_cuts_GPU (.cu:2844-2868); keep[i] = passed */
-__global__ void __launch_bounds__(256) k_cuts(int64_t n, HistView h, int K, const float* __restrict__ mw,
-                                              const float* __restrict__ mut, const float* __restrict__ muv,
-                                              const float* __restrict__ sw, const float* __restrict__ sut,
-                                              const float* __restrict__ suv, uint8_t* __restrict__ keep,
-                                              int* __restrict__ counts_post, long long* __restrict__ sino_sum) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int b = h.bin_num[i];
-    double rut = dev_rel_angle(h.xy_exit_angle[i], h.xy_entry_angle[i]);
-    double ruv = dev_rel_angle(h.xz_exit_angle[i], h.xz_entry_angle[i]);
-    float w = h.wepl[i];
-    int p_ut = fabs(rut - mut[b]) < (K * sut[b]);
-    int p_uv = fabs(ruv - muv[b]) < (K * suv[b]);
-    int p_w = fabsf(mw[b] - w) <= (K * sw[b]);
-    int f = !p_ut || !p_uv || !p_w;
-    h.failed[i] = (uint8_t)f;
-    keep[i] = (uint8_t)!f;
-    if (!f) {
-        atomicAdd(counts_post + b, 1);
-        dev_add_fixed(sino_sum + b, dev_to_fixed(w, PCT_SCALE_WEPL));
-    }
-}
-
-/* construct_sinogram_GPU (.cu:2912-2917) */
-__global__ void k_sinogram(int nb, const int* __restrict__ counts_post, const long long* __restrict__ sino_sum,
-                           float* __restrict__ sino) {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    float s = dev_from_fixed(sino_sum[b], PCT_SCALE_WEPL);
-    if (counts_post[b] > 0) s /= counts_post[b];
-    sino[b] = s;
+    /* binning counts (.cu:2551-2567); the sums follow in history order */
+    if (!m && valid) atomicAdd(counts + bin, 1);
 }
 
 }  // namespace
@@ -302,19 +199,15 @@ static pct_status ensure_tables(pct_ctx* c) {
     return PCT_OK;
 }
 
-static pct_status ensure_bins(pct_ctx* c) {
+pct_status pct_ensure_bins(pct_ctx* c) {
     if (c->bin_counts.p) return PCT_OK;
     size_t nb = (size_t)c->geo.num_bins;
     PCT_TRY(c->bin_counts.alloc(nb * 4));
     PCT_TRY(c->bin_counts_post.alloc(nb * 4));
-    PCT_TRY(c->bin_sum1.alloc(nb * 3 * 8));
-    PCT_TRY(c->bin_sum2.alloc(nb * 3 * 8));
-    PCT_TRY(c->sino_sum.alloc(nb * 8));
     DevBuf* f[] = {&c->mean_wepl, &c->mean_ut, &c->mean_uv, &c->sd_wepl, &c->sd_ut, &c->sd_uv, &c->sinogram,
                    &c->sinogram_filtered};
     for (DevBuf* b : f) PCT_TRY(b->alloc(nb * 4));
     PCT_CUDA(cudaMemsetAsync(c->bin_counts.p, 0, nb * 4, c->stream));
-    PCT_CUDA(cudaMemsetAsync(c->bin_sum1.p, 0, nb * 3 * 8, c->stream));
     return PCT_OK;
 }
 
@@ -328,7 +221,7 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
         return PCT_OK;
     }
     PCT_TRY(ensure_tables(c));
-    PCT_TRY(ensure_bins(c));
+    PCT_TRY(pct_ensure_bins(c));
     PCT_TRY(pct_hull_images_ready(c));
     In13 in;
     const float* d_angle = angle;
@@ -351,7 +244,7 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
      * of a part on the context stream, its hull walks (hull_detection, .cu:100)
      * on the second stream once the part is preprocessed, so that the binary32
      * walks of one part overlap the binary64 preprocessing of the next.  The
-     * images are integer counts and the bin sums exact: the order of the parts
+     * images and the bin counts are integer counts: the order of the parts
      * does not change them. */
     const int parts = n >= ((int64_t)1 << 22) ? PIPE_PARTS : 1;
     const int64_t part = (n + parts - 1) / parts;
@@ -378,7 +271,7 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
         ++c->launches;
         k_preprocess<<<pct_grid_for(m, 256), 256, 0, c->stream>>>(
             c->dg, ink, d_angle + a, m, c->trig_gantry.as<double2>(), c->trig_bins.as<double2>(),
-            hv_offset(stage, a), missed + a, c->bin_counts.as<int>(), c->bin_sum1.as<long long>(), 0);
+            hv_offset(stage, a), missed + a, c->bin_counts.as<int>());
         if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ev[k], c->stream) != cudaSuccess ||
             cudaStreamWaitEvent(c->stream2, ev[k], 0) != cudaSuccess) {
             st = pct_fail(PCT_ERR_CUDA, "process_chunk: preprocessing launch");
@@ -401,48 +294,5 @@ pct_status pct_stage_process_chunk(pct_ctx* c, const float* const data13[13], co
     c->counts.total_histories += n;
     c->counts.recon_vol_histories += kept;
     c->stage = ST_BINNED;
-    return PCT_OK;
-}
-
-pct_status pct_stage_cuts(pct_ctx* c) {
-    if (c->stage < ST_BINNED) return pct_fail(PCT_ERR_STATE, "statistical_cuts before any chunk");
-    if (c->stage >= ST_CUT) return pct_fail(PCT_ERR_STATE, "statistical_cuts already done");
-    PCT_TRY(ensure_bins(c));
-    const int nb = c->geo.num_bins;
-    const int64_t n = c->h.n;
-    HistView h = c->view(c->h);
-    ++c->launches;
-    k_means<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts.as<int>(), c->bin_sum1.as<long long>(),
-                                                          c->mean_wepl.as<float>(), c->mean_ut.as<float>(),
-                                                          c->mean_uv.as<float>());
-    PCT_CUDA(cudaMemsetAsync(c->bin_sum2.p, 0, (size_t)nb * 3 * 8, c->stream));
-    if (n > 0) {
-        ++c->launches;
-        k_sq_dev<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, h, c->mean_wepl.as<float>(), c->mean_ut.as<float>(),
-                                                               c->mean_uv.as<float>(), c->bin_sum2.as<long long>());
-    }
-    ++c->launches;
-    k_sigma<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts.as<int>(), c->bin_sum2.as<long long>(),
-                                                          c->cfg.sample_std_dev ? 1 : 0, c->sd_wepl.as<float>(),
-                                                          c->sd_ut.as<float>(), c->sd_uv.as<float>());
-    PCT_CUDA(cudaMemsetAsync(c->bin_counts_post.p, 0, (size_t)nb * 4, c->stream));
-    PCT_CUDA(cudaMemsetAsync(c->sino_sum.p, 0, (size_t)nb * 8, c->stream));
-    PCT_TRY(c->tmp_missed.alloc(n > 0 ? n : 1));
-    uint8_t* keep = c->tmp_missed.as<uint8_t>();
-    if (n > 0) {
-        ++c->launches;
-        k_cuts<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(
-            n, h, c->cfg.sigmas_to_keep, c->mean_wepl.as<float>(), c->mean_ut.as<float>(), c->mean_uv.as<float>(),
-            c->sd_wepl.as<float>(), c->sd_ut.as<float>(), c->sd_uv.as<float>(), keep, c->bin_counts_post.as<int>(),
-            c->sino_sum.as<long long>());
-    }
-    ++c->launches;
-    k_sinogram<<<pct_grid_for(nb, 256), 256, 0, c->stream>>>(nb, c->bin_counts_post.as<int>(),
-                                                             c->sino_sum.as<long long>(), c->sinogram.as<float>());
-    PCT_CUDA(cudaGetLastError());
-    int64_t kept = 0;
-    PCT_TRY(pct_compact_histories(c, keep, n, &kept));
-    c->counts.post_cut_histories = kept;
-    c->stage = ST_CUT;
     return PCT_OK;
 }

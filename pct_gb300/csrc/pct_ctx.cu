@@ -308,7 +308,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->stream2) cudaStreamSynchronize(c->stream2);
     DevBuf* all[] = {&c->dense_off, &c->dense_rows, &c->row_len, &c->in_angle, &c->tmp_missed, &c->tmp_hist, &c->scan_tmp, &c->pinned_count, &c->bin_counts,
-                     &c->bin_counts_post, &c->bin_sum1, &c->bin_sum2, &c->sino_sum, &c->mean_wepl, &c->mean_ut,
+                     &c->bin_counts_post, &c->bin_sort, &c->bin_seg, &c->mean_wepl, &c->mean_ut,
                      &c->mean_uv, &c->sd_wepl, &c->sd_ut, &c->sd_uv, &c->sinogram, &c->sinogram_filtered,
                      &c->filter_taps, &c->filter_scale, &c->trig_gantry, &c->trig_bins, &c->err_flags,
                      &c->sc_hull, &c->msc_counts, &c->sm_counts, &c->msc_hull, &c->sm_hull, &c->fbp_image,

@@ -7,8 +7,9 @@
  *                   bin (int32), flags (uint8), first voxel (uint32).  It is
  *                   compacted in place after binning, cuts and endpoints,
  *                   like the reference's *_vector globals.
- *   bins            counts (int32), exact fixed-point sums (int64) and the
- *                   binary32 means / sigmas / sinogram (NUM_BINS each).
+ *   bins            counts (int32) and the binary32 means / sigmas /
+ *                   sinogram (NUM_BINS each); while the cuts run, the store
+ *                   order sorted by bin (stable) and each bin's segment of it.
  *   voxels          hull count images (int32), hull masks (uint8), FBP
  *                   image, iterate x, DROP update accumulator (float).
  *   MLP rows        row offsets (int64, R+1), voxel entries (uint32), chord
@@ -130,7 +131,8 @@ struct pct_ctx {
     HistoryStore h, h2;            /* h2: scratch store for out-of-place compaction */
 
     /* bins */
-    DevBuf bin_counts, bin_counts_post, bin_sum1, bin_sum2, sino_sum;
+    DevBuf bin_counts, bin_counts_post;
+    DevBuf bin_sort, bin_seg;      /* statistics: stable sort of the store by bin, per-bin segments */
     DevBuf mean_wepl, mean_ut, mean_uv, sd_wepl, sd_ut, sd_uv, sinogram, sinogram_filtered;
     DevBuf filter_taps, filter_scale, trig_gantry, trig_bins;
     DevBuf err_flags;              /* device error/overflow counters */

@@ -1,6 +1,7 @@
 /*
  * Device helpers shared by the kernels: voxel arithmetic of the reference
- * walks and the exact fixed-point bin sums.
+ * walks, the brick voxel order, certified binary32 walk arithmetic and block
+ * scans.
  *
  * The voxel helpers evaluate the reference's expressions
  * (src/pCT_Reconstruction_Data_Segments.cu:8508-8752) in binary64 in source
@@ -34,24 +35,6 @@ __device__ __forceinline__ double dev_distance_remaining(double zero, double pos
 /* corresponding_coordinate_GPU (.cu:8748) */
 __device__ __forceinline__ double dev_corresponding(double m, double x, double x0, double y0) {
     return m * (x - x0) + y0;
-}
-
-/* Exact per-bin sums: binary32 summands in fixed point (2^32 for WEPL and
- * squared WEPL deviations, 2^40 for angles, 2^48 for squared angle
- * deviations); integer addition makes the sum independent of order. */
-#define PCT_SCALE_WEPL 4294967296.0
-#define PCT_SCALE_ANGLE 1099511627776.0
-#define PCT_SCALE_ANGLE_SQ 281474976710656.0
-
-__device__ __forceinline__ long long dev_to_fixed(float v, double scale) {
-    double s = (double)v * scale;
-    return (long long)(s >= 0 ? s + 0.5 : s - 0.5);
-}
-__device__ __forceinline__ void dev_add_fixed(long long* dst, long long v) {
-    atomicAdd((unsigned long long*)dst, (unsigned long long)v);
-}
-__host__ __device__ __forceinline__ float dev_from_fixed(long long s, double scale) {
-    return (float)((double)s / scale);
 }
 
 /* relative angle with the +-2 pi wrap (.cu:2557-2566) */
@@ -184,6 +167,33 @@ __global__ void __launch_bounds__(1024) k_chunk_order(int64_t n, const K* __rest
 #pragma unroll
     for (int r = 0; r < PER; ++r)
         if (kk[r] >= 0) order[base + cnt[kk[r]] + rank[r]] = (uint32_t)(base + threadIdx.x + r * 1024);
+}
+
+/* Exclusive scan of one value per thread over the CTA (blockDim.x a multiple
+ * of 32, at most 1024); ws holds 32 words of shared memory; *total receives the
+ * CTA's sum.  Every thread of the CTA must call it. */
+__device__ __forceinline__ uint32_t dev_block_exclusive_scan_u32(uint32_t v, uint32_t* ws, uint32_t* total) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        ws[lane] = s;
+    }
+    __syncthreads();
+    uint32_t r = x - v + (w > 0 ? ws[w - 1] : 0u);
+    *total = ws[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return r;
 }
 
 static inline unsigned pct_grid_for(int64_t n, int threads) {

@@ -87,7 +87,7 @@ def test_block_size_extremes_against_oracle(block):
     w = phantoms.tiny(num_histories=20000, seed=6, v_extent=0.3)
     cfg = _cfg(w, iterations=1, block_size=block)
     data, angles = phantoms.generate(w)
-    ora = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_EXACT, iterations=1)
+    ora = oracle.run_pipeline(cfg, data, angles, iterations=1)
     r = _through_rows(cfg, data, angles)
     r.drop(1)
     x = r.array("X").astype(np.float64)
@@ -102,7 +102,7 @@ def test_odd_grid_without_bricks_against_oracle():
     g = phantoms.geometry(cfg)
     assert g.num_voxels % 4 != 0 and g.columns % 4 != 0
     data, angles = phantoms.generate(w)
-    ora = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_EXACT, iterations=2, keep_history=True)
+    ora = oracle.run_pipeline(cfg, data, angles, iterations=2, keep_history=True)
     r = _through_rows(cfg, data, angles)
     offs, rows, _ = oracle.mlp_rows(cfg, ora["_hr"])
     assert np.array_equal(r.array("ROW_OFFSETS"), offs)

@@ -1,9 +1,9 @@
 """CUDA path vs the CPU oracle, stage by stage (needs a GPU).
 
 Bit-exact: per-history intersections and bins, hull counts and hulls, bin
-means/sigmas (both sides use exact bin sums), cut masks, sinogram, filtered
-sinogram, FBP image, hull selection, initial iterate, MLP endpoints and MLP
-voxel rows.  DROP: the binary32 GPU iterate against the oracle's binary64 run
+means/sigmas (both sides add the reference's binary32 sums in history order),
+cut masks, sinogram, filtered sinogram, FBP image, hull selection, initial
+iterate, MLP endpoints and MLP voxel rows.  DROP: the binary32 GPU iterate against the oracle's binary64 run
 of the same iterations, relative L2 <= 1e-4.
 """
 import numpy as np
@@ -24,6 +24,8 @@ CASES = {
     "tiny_clip": lambda: (phantoms.tiny(num_histories=40000, seed=11, v_extent=0.55), {}),
     "tiny_drop": lambda: (phantoms.tiny(num_histories=40000, seed=7, v_extent=0.3), {}),
     "cfg1_sm": lambda: (phantoms.cfg1(num_histories=120000, seed=5), dict(iterations=2)),
+    # the benchmark's grid and phantom: 256x256x32 voxels, 180 angles
+    "cfg2_grid": lambda: (phantoms.cfg2(num_histories=200000, seed=9), dict(iterations=2, block_size=50000)),
     # config 3 grids at both ends: ellipsoid phantoms on 128x128x8 and 256x256x48
     "cfg3_128x8": lambda: (phantoms.ellipsoids(31, num_histories=150000, cols=128, slices=8),
                            dict(iterations=2, block_size=50000)),
@@ -52,7 +54,7 @@ def run(request):
     cfg_over.update(over)
     cfg = phantoms.make_config(cfg_over)
     data, angles = phantoms.generate(w)
-    ora = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_EXACT, keep_history=True)
+    ora = oracle.run_pipeline(cfg, data, angles, keep_history=True)
     r = recon.Reconstruction(cfg)
     out = {}
     # three chunks of unequal size: the resident store must come out as one batch would

@@ -60,7 +60,7 @@ def oracle_outputs(fx):
     for k in ("msc_on", "sm_on", "sc_on", "mlp_hull"):
         if k in run:
             setattr(cfg, k, run[k])
-    out = oracle.run_pipeline(cfg, data, angles, sum_mode=oracle.SUM_SEQUENTIAL, iterations=run.get("iterations", 0),
+    out = oracle.run_pipeline(cfg, data, angles, iterations=run.get("iterations", 0),
                               block_size=run.get("block_size", 3200), lam=float(np.float32(run.get("lambda_", 0.001))),
                               keep_history=True)
     # names of the reference captures that the oracle produces under another name
