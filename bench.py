@@ -18,8 +18,8 @@ DROP, then reading the image back), per step.
   python bench.py [--steps K] [--warmup W] [--histories N] [--impl reference]
 
 With --impl reference the step is the reference algorithm on the CPU (the C
-restatement in oracle/, all host threads for the MLP rows and the DROP row
-updates) on a bounded sample of the same workload.
+restatement in oracle/, all host threads) on one full DROP block of the same
+workload: its MLP rows and the 12 DROP iterations over it.
 Under torchrun (N > 1) every rank runs the same workload on its own GPU
 (replicas: the path has no cross-GPU exchange here) and `value` sums them.
 """
@@ -54,7 +54,7 @@ def parse():
                     help="round chords to bfloat16 (default: the workload's setting; cfg4 uses bf16)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--cpu-sample", type=int, default=6000)
+    ap.add_argument("--cpu-sample", type=int, default=60000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--drop-form", type=int, default=0, choices=[0, 1, 2],
                     help="DROP block step: 0 scatter (default), 1 sorted, 2 tiled")
@@ -179,40 +179,86 @@ def time_oracle(cfg, h, x0, iterations, threads):
     return n * iterations / dt, dt, n
 
 
+def mapped_repo_libraries():
+    """Shared libraries of this repository mapped into the process (from /proc/self/maps)."""
+    found = set()
+    try:
+        for line in open("/proc/self/maps"):
+            path = line.split()[-1] if len(line.split()) >= 6 else ""
+            if path.endswith(".so") and path.startswith(ROOT):
+                found.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(found)
+
+
+def workload(a, rank):
+    """The scan of this run (seeded per rank) and its configuration overrides."""
+    from pct_gb300 import phantoms  # workload definitions (no library is mapped)
+    make_workload = phantoms.cfg4 if a.workload == "cfg4" else phantoms.cfg2
+    w = make_workload(num_histories=a.histories, seed=(4 if a.workload == "cfg4" else 2) + rank)
+    over = dict(w.config)
+    if a.chord_bf16 is not None:
+        over["chord_bf16"] = a.chord_bf16
+    over["drop_form"] = a.drop_form
+    over["voxel_order"] = a.voxel_order
+    return w, over
+
+
+def describe(a, w, cfg, g, n, R):
+    return ("%s: %d histories, %d recon histories, %d angles, %dx%dx%d, %d DROP iterations, block %d, lambda %.2g,"
+            " %s chords" % (a.workload, n, R, w.num_angles, g.columns, g.rows, g.slices, cfg.iterations,
+                            cfg.block_size, cfg.lambda_, "bf16" if cfg.chord_bf16 else "binary32"))
+
+
 def run_reference_arm(a, ws, rank):
-    """--impl reference: the reference algorithm on the CPU, bounded sample per step."""
+    """--impl reference: the reference algorithm on the host cores, on this bench's workload.
+
+    Setup, untimed: the C restatement of the reference's main() sequence (oracle/) on the
+    whole scan: preprocessing, hulls, cuts, FBP, initial iterate, hull endpoints.  A step:
+    the MLP rows of the first DROP block (block_size recon histories, one full block) and
+    the DROP iterations over that block, on all host threads.  The histories come from the
+    host build of the seeded generator, so no CUDA library is mapped by this arm."""
     if rank != 0:
         return
-    from pct_gb300 import phantoms
     from oracle import oracle
-    w = phantoms.cfg2(num_histories=min(a.histories, 1_500_000))
-    cfg = phantoms.make_config(w.config)
-    data, angles = phantoms.generate(w)
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    w, over = workload(a, 0)
+    cfg = oracle.make_config(over)
+    g = oracle.geometry(cfg)
+    data, angles = oracle.generate(w)
+    n = data.shape[1]
+    t0 = time.perf_counter()
     ora = oracle.run_pipeline(cfg, data, angles, iterations=0, keep_history=True)
+    setup_s = time.perf_counter() - t0
+    del data, angles
     hr = ora["_hr"]
-    sample = min(len(hr["WEPL"]), 40000)
+    R = len(hr["WEPL"])
+    sample = min(R, cfg.block_size)
     h = {k: v[:sample].copy() for k, v in hr.items()}
     x0 = ora["x_k0"].astype(np.float64)
+    del ora, hr
+    iters = cfg.iterations
     for _ in range(a.warmup):
-        time_oracle(cfg, h, x0, cfg.iterations, threads)
+        time_oracle(cfg, h, x0, iters, threads)
     times = []
     for _ in range(a.steps):
-        v, dt, n = time_oracle(cfg, h, x0, cfg.iterations, threads)
+        v, dt, _ = time_oracle(cfg, h, x0, iters, threads)
         times.append(dt)
-    value = sample * cfg.iterations * a.steps / sum(times)
+    value = sample * iters * a.steps / sum(times)
     cpu, ncores = host_info()
+    sample_text = ("the first DROP block (%d of %d recon histories) per step: its MLP rows and %d DROP iterations "
+                   "over it, on %d threads of %s; setup (preprocessing .. endpoints of the whole scan) %.1f s, "
+                   "untimed" % (sample, R, iters, threads, cpu, setup_s))
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
            "ms_per_step": 1e3 * sum(times) / a.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded phantom generator, PCTD layout)",
            "impl": "reference",
-           "config": {"workload": "cfg2 geometry 256x256x32, 12 DROP iterations, block 200000, lambda 0.1; "
-                                  "CPU sample of %d recon histories per step" % sample},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": "%d recon histories x %d iterations per step (MLP rows + DROP), %s"
-                                      % (sample, cfg.iterations, cpu)},
-           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": {"workload": describe(a, w, cfg, g, n, R), "sample": sample_text},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_text},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "libraries_mapped": mapped_repo_libraries()}
     print(json.dumps(out))
 
 
@@ -231,13 +277,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    make_workload = phantoms.cfg4 if a.workload == "cfg4" else phantoms.cfg2
-    w = make_workload(num_histories=a.histories, seed=(4 if a.workload == "cfg4" else 2) + rank)
-    over = dict(w.config)
-    if a.chord_bf16 is not None:
-        over["chord_bf16"] = a.chord_bf16
-    over["drop_form"] = a.drop_form
-    over["voxel_order"] = a.voxel_order
+    w, over = workload(a, rank)
     cfg = phantoms.make_config(over)
     iters = cfg.iterations
     data, angles = phantoms.generate(w)
@@ -378,17 +418,29 @@ def main():
 
     r.reset_iterate()
     r.mlp_rows()
-    errs = [errors(r.array("X"))]
+    xs = [r.array("X")]
+    errs = [errors(xs[0])]
     for _ in range(iters):
         r.drop(1)
-        errs.append(errors(r.array("X")))
+        xs.append(r.array("X"))
+        errs.append(errors(xs[-1]))
+    # the binary32 iterates against a binary64 run of the same iterations on the same rows
+    x64 = xs[0].astype(np.float64)
+    fp64_err = []
+    for k in range(iters):
+        x64, _ = r.drop_fp64(1, x64)
+        fp64_err.append(float(np.linalg.norm(xs[k + 1] - x64) / np.linalg.norm(x64)))
+    del xs
     hit = next((k for k, e in enumerate(errs) if e[0] <= 0.5), None)
     accuracy = {"region_mean_rsp_error_pct_per_iteration": [e[0] for e in errs],
                 "voxel_rsp_rmse_pct_per_iteration": [e[1] for e in errs],
                 "regions": "%d materials, %d voxels at least 3 voxels (in-slice) from a material boundary"
                            % (len(mats), int(sum(m.sum() for _, m in mats))),
                 "start": "FBP x hull (iteration 0)",
-                "seconds_to_region_error_0.5pct": (mlp_s / a.steps + hit * drop_iter_s) if hit is not None else None}
+                "seconds_to_region_error_0.5pct": (mlp_s / a.steps + hit * drop_iter_s) if hit is not None else None,
+                "fp64_rel_l2_per_iteration": fp64_err,
+                "fp64_reference": "pct_drop_fp64: the same iterations on the same rows with binary64 chord, dot, "
+                                  "update sums and iterate (relative L2 of the binary32 iterate against it)"}
 
     # ---- end to end through the public API with host buffers --------------------------
     pinned = torch.empty((13, n), dtype=torch.float32, pin_memory=True)
@@ -432,10 +484,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": t / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded phantom generator, PCTD layout)",
-            "config": {"workload": "%s: %d histories, %d recon histories, %d angles, %dx%dx%d, %d DROP iterations,"
-                                   " block %d, lambda %.2g, %s chords"
-                                   % (a.workload, n, R, w.num_angles, g.columns, g.rows, g.slices, iters,
-                                      cfg.block_size, cfg.lambda_, "bf16" if cfg.chord_bf16 else "binary32"),
+            "config": {"workload": describe(a, w, cfg, g, n, R),
                        "row_entries": rows, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "inputs larger than L2 (MLP rows %.1f GB)" % (rows * 4 / 1e9),
                        "drop_form": forms[a.drop_form], "drop_form_ran": forms.get(form_ran, str(form_ran)),

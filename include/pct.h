@@ -252,6 +252,15 @@ pct_status pct_mlp_rows(pct_ctx* ctx);
  * image_reconstruction_GPU, src/pCT_Reconstruction_Data_Segments.cu:6795-6860).
  * stats may be NULL. */
 pct_status pct_drop(pct_ctx* ctx, int iterations, pct_drop_stats* stats);
+/* Binary64 DROP on the resident rows: `iterations` iterations of the same
+ * block update with every quantity in binary64 (the chord, dot, ||a_i||^2,
+ * update accumulator and iterate), as the reference's host DROP_blocks /
+ * DROP_update keep them (src/pCT_Reconstruction_Data_Segments.cu:8023-8055).
+ * x: host array of NUM_VOXELS doubles (linear voxel order), the start image
+ * in and the result out; the context's binary32 iterate is not touched.  For
+ * the error of pct_drop against a binary64 run of the same iterations; needs
+ * the scatter or sorted form and the standard update.  stats may be NULL. */
+pct_status pct_drop_fp64(pct_ctx* ctx, int iterations, double* x, pct_drop_stats* stats);
 /* image_reconstruction_GPU (pCT_functions.h:237): endpoints, rows, all
  * cfg->iterations DROP iterations. */
 pct_status pct_image_reconstruction(pct_ctx* ctx, pct_drop_stats* stats);

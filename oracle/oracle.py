@@ -56,8 +56,47 @@ def _cfgp(cfg):
 
 
 def geometry(cfg):
-    from pct_gb300 import phantoms
-    return phantoms.geometry(cfg)
+    g = _capi.Geometry()
+    assert load().ora_geometry(_cfgp(cfg), C.byref(g)) == 0, "invalid geometry"
+    return g
+
+
+def make_config(overrides):
+    """pct_config with the reference's defaults and the given overrides (no CUDA library)."""
+    cfg = _capi.Config()
+    load().ora_config_default(C.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+_gen = None
+
+
+def generate(w):
+    """The seeded histories of workload `w` (pct_gb300.phantoms) from the host-only build of the
+    generator: ((13, N) float32 PCTD arrays in mm, (N,) float32 projection angles), the same bits
+    as phantoms.generate without mapping the CUDA library."""
+    global _gen
+    if _gen is None:
+        _gen = C.CDLL(build_oracle.build_gen())
+        _gen.pct_gen_last_error.restype = C.c_char_p
+    n = int(w.num_histories)
+    data = np.empty((13, n), dtype=np.float32)
+    angles = np.empty(n, dtype=np.float32)
+    sp = _capi.ScanParams(seed=w.seed, num_angles=w.num_angles, gantry_angle_interval=w.gantry_angle_interval,
+                          t_extent=w.t_extent, v_extent=w.v_extent, source_radius=260.7,
+                          angular_spread=w.angular_spread, beam_energy_mev=200.0, wepl_noise=w.wepl_noise,
+                          outlier_fraction=w.outlier_fraction, outlier_max=w.outlier_max,
+                          scatter_scale=w.scatter_scale)
+    objs = (_capi.PhantomObject * max(1, len(w.objects)))()
+    for i, o in enumerate(w.objects):
+        objs[i] = _capi.PhantomObject(*o)
+    ptrs = (C.c_void_p * 13)(*[data[k].ctypes.data for k in range(13)])
+    rc = _gen.pct_generate_histories(objs, len(w.objects), C.byref(sp), ptrs, C.c_void_p(angles.ctypes.data),
+                                     C.c_int64(n))
+    assert rc == 0, _gen.pct_gen_last_error().decode(errors="replace")
+    return data, angles
 
 
 HIST_FIELDS = ["x_entry", "y_entry", "z_entry", "x_exit", "y_exit", "z_exit",

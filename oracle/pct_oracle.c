@@ -21,6 +21,14 @@
 
 int ora_version(void) { return 1; }
 
+/* The configuration defaults of pCT_config.h / pCT_data.h (pct_geometry.h), so
+ * that a caller of the oracle needs no other library. */
+int ora_config_default(pct_config* cfg) {
+    pct_config_fill_defaults(cfg);
+    return 0;
+}
+int ora_geometry(const pct_config* cfg, pct_geometry* g) { return pct_geometry_derive(cfg, g); }
+
 /* ------------------------------------------------------------------------- */
 /* shared geometry helpers (.cu:8508-8867)                                    */
 /* ------------------------------------------------------------------------- */
@@ -375,6 +383,9 @@ int ora_hull_walk(const pct_config* cfg, int kind, int64_t n, const uint8_t* mis
     if (pct_geometry_derive(cfg, &g)) return 1;
     const int cap = 4 * (g.columns + g.rows + g.slices) + 16;
     int64_t capped = 0, outside = 0;
+    /* Histories walk in parallel; the image updates are integer adds (or stores
+     * of 0), so the result does not depend on their order. */
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : capped, outside)
     for (int64_t i = 0; i < n; ++i) {
         int use;
         if (kind == 0) use = !missed[i] && (wepl[i] <= cfg->sc_threshold);
@@ -410,8 +421,13 @@ int ora_hull_walk(const pct_config* cfg, int kind, int64_t n, const uint8_t* mis
         for (;;) {
             if (!end) {
                 if (w.voxel >= 0 && w.voxel < g.num_voxels) {
-                    if (kind == 0) image[w.voxel] = 0;
-                    else image[w.voxel] += 1;
+                    if (kind == 0) {
+#pragma omp atomic write
+                        image[w.voxel] = 0;
+                    } else {
+#pragma omp atomic update
+                        image[w.voxel] += 1;
+                    }
                 } else {
                     ++outside;
                 }
@@ -535,6 +551,7 @@ void ora_filter(const pct_config* cfg, const float* sinogram, float* filtered) {
     if (pct_geometry_derive(cfg, &g)) return;
     const double TB = cfg->t_bin_size, VB = cfg->v_bin_size, SR = cfg->source_radius;
     const double tau = (double)(2 / sqrtf(2.0f)) * TB; /* RAM_LAK_TAU = 2/ROOT_TWO * T_BIN_SIZE (pCT_data.h:247) */
+#pragma omp parallel for collapse(2) schedule(static)
     for (int vb = 0; vb < g.v_bins; ++vb)
         for (int ab = 0; ab < g.angular_bins; ++ab) {
             int strip = (vb * g.angular_bins * g.t_bins) + (ab * g.t_bins);

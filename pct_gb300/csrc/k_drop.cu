@@ -296,7 +296,7 @@ __global__ void k_image_from_brick(DevGeom g, const float* __restrict__ brk, flo
 /* Per-block voxel counts for the scatter form. */
 /* Number of DROP blocks: of this context's rows, or of the global rows when the
  * rows are one shard of a sharded DROP (every rank runs every block). */
-static int drop_num_blocks(const pct_ctx* c) {
+int pct_drop_num_blocks(const pct_ctx* c) {
     const int64_t B = c->cfg.block_size;
     if (c->num_shards > 1) {
         const int64_t Bg = B * c->num_shards;
@@ -306,7 +306,7 @@ static int drop_num_blocks(const pct_ctx* c) {
 }
 
 /* Rows [s, e) of block k (empty past the end of a shard). */
-static void drop_block_range(const pct_ctx* c, int k, int64_t* s, int64_t* e) {
+void pct_drop_block_range(const pct_ctx* c, int k, int64_t* s, int64_t* e) {
     const int64_t n = c->h.n, B = c->cfg.block_size;
     const int64_t a = (int64_t)k * B;
     *s = a < n ? a : n;
@@ -325,12 +325,12 @@ static pct_status drop_allreduce(pct_ctx* c, void* data, int64_t count, int dtyp
 
 static pct_status build_scatter(pct_ctx* c) {
     const int nv = c->geo.num_voxels;
-    int nb = drop_num_blocks(c);
+    int nb = pct_drop_num_blocks(c);
     PCT_TRY(c->block_diag.alloc(sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1)));
     PCT_CUDA(cudaMemsetAsync(c->block_diag.p, 0, sizeof(uint32_t) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
     for (int k = 0; k < nb; ++k) {
         int64_t s, e;
-        drop_block_range(c, k, &s, &e);
+        pct_drop_block_range(c, k, &s, &e);
         if (e == s) continue;
         ++c->launches;
         k_block_counts<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
@@ -342,7 +342,7 @@ static pct_status build_scatter(pct_ctx* c) {
         PCT_CUDA(cudaMemsetAsync(c->block_norm.p, 0, sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
         for (int k = 0; k < nb; ++k) {
             int64_t s, e;
-            drop_block_range(c, k, &s, &e);
+            pct_drop_block_range(c, k, &s, &e);
             if (e == s) continue;
             ++c->launches;
             k_block_norms<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
@@ -368,7 +368,7 @@ static pct_status build_sorted(pct_ctx* c) {
     const int64_t n = c->h.n;
     const uint32_t nkeys = (uint32_t)c->geo.num_bins;
     const int tiles = (int)((nkeys + SCAN_TILE - 1) / SCAN_TILE);
-    int nb = drop_num_blocks(c);
+    int nb = pct_drop_num_blocks(c);
     PCT_TRY(c->drop_perm.alloc(sizeof(uint32_t) * (n > 0 ? n : 1)));
     PCT_TRY(c->drop_sort.alloc(sizeof(uint32_t) * ((size_t)2 * nkeys + tiles)));
     uint32_t* cnt = c->drop_sort.as<uint32_t>();
@@ -378,7 +378,7 @@ static pct_status build_sorted(pct_ctx* c) {
     uint32_t* perm = c->drop_perm.as<uint32_t>();
     for (int k = 0; k < nb; ++k) {
         int64_t s, e;
-        drop_block_range(c, k, &s, &e);
+        pct_drop_block_range(c, k, &s, &e);
         if (e == s) continue;
         PCT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * nkeys, c->stream));
         c->launches += 5;
@@ -410,7 +410,7 @@ static unsigned drop_rows_grid(pct_ctx* c, int64_t rows, const void* fn) {
  * residual accumulator; returns the number of launches. */
 static int enqueue_block_rows(pct_ctx* c, int k, double* resid) {
     int64_t s, e;
-    drop_block_range(c, k, &s, &e);
+    pct_drop_block_range(c, k, &s, &e);
     if (e == s) return 0;
     const int nv = c->geo.num_voxels;
     const uint32_t* perm = c->drop_mode == PCT_DROP_SORTED ? c->drop_perm.as<uint32_t>() : nullptr;
@@ -484,10 +484,9 @@ static pct_status capture_iteration(pct_ctx* c, double* acc) {
     return PCT_OK;
 }
 
-pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
-    if (c->stage != ST_ROWS) return pct_fail(PCT_ERR_STATE, "drop needs MLP rows");
-    if (iterations < 0) return pct_fail(PCT_ERR_ARGUMENT, "drop: negative iteration count");
-    const int nv = c->geo.num_voxels;
+/* Builds the per-block structures of the configured DROP form once per set of
+ * rows and block size (diagonal counts; sort order; tiled segments). */
+pct_status pct_drop_prepare(pct_ctx* c) {
     if (!c->diag_ready) {
         pct_drop_release_graph(c);
         c->td.release();
@@ -508,6 +507,14 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
             PCT_TRY(build_scatter(c));
         }
     }
+    return PCT_OK;
+}
+
+pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
+    if (c->stage != ST_ROWS) return pct_fail(PCT_ERR_STATE, "drop needs MLP rows");
+    if (iterations < 0) return pct_fail(PCT_ERR_ARGUMENT, "drop: negative iteration count");
+    const int nv = c->geo.num_voxels;
+    PCT_TRY(pct_drop_prepare(c));
     PCT_TRY(c->x_update.alloc(sizeof(float) * nv));
     PCT_CUDA(cudaMemsetAsync(c->x_update.p, 0, sizeof(float) * nv, c->stream));
     const bool brick = c->dg.brick && c->drop_mode != PCT_DROP_TILED;

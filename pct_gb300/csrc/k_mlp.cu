@@ -1162,7 +1162,27 @@ __global__ void k_tile_scan64(const int64_t* __restrict__ len, int64_t n, const 
     if (i == 0) off[n] = *total;
 }
 
+/* The binary64 chord of every row (bf16: rounded to bfloat16 first), for the
+ * binary64 DROP. */
+__global__ void k_row_chords64(DevGeom g, int64_t n, HistView h, int bf16, double* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ae = h.xy_entry_angle[i], ax = h.xy_exit_angle[i], ze = h.xz_entry_angle[i], zx = h.xz_exit_angle[i];
+    double c = dev_chord(g, (ae + ax) / 2.0, (ze + zx) / 2.0);
+    if (bf16) c = (double)__bfloat162float(__float2bfloat16_rn((float)c));
+    out[i] = c;
+}
+
 }  // namespace
+
+pct_status pct_row_chords64(pct_ctx* c, double* out) {
+    const int64_t n = c->h.n;
+    if (n == 0) return PCT_OK;
+    ++c->launches;
+    k_row_chords64<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(c->dg, n, c->view(c->h), c->cfg.chord_bf16, out);
+    PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
 
 pct_status pct_stage_endpoints(pct_ctx* c) {
     if (c->stage != ST_X0) return pct_fail(PCT_ERR_STATE, "collect_mlp_endpoints needs the initial iterate");

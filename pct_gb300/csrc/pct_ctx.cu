@@ -315,7 +315,8 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
                      &c->rows, &c->chord, &c->row_scale, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
                      &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order, &c->walk_order, &c->mlp_tab_trig, &c->mlp_tab_depth,
-                     &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm};
+                     &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm,
+                     &c->d64_x, &c->d64_upd, &c->d64_chord, &c->d64_res};
     for (DevBuf* b : all) b->release();
     c->td.release();
     for (auto& b : c->in13) b.release();

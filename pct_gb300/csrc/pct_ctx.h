@@ -153,6 +153,7 @@ struct pct_ctx {
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
     int64_t dense_total = 0;
     DevBuf drop_resid;
+    DevBuf d64_x, d64_upd, d64_chord, d64_res;  /* binary64 DROP (pct_drop_fp64) */
     cudaGraphExec_t drop_graph_exec = nullptr;  /* one DROP iteration */
     int64_t row_capacity = 0;
     int num_blocks = 0;

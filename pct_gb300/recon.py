@@ -62,6 +62,7 @@ def _declare(lib):
         getattr(lib, name).argtypes = [vp]
     lib.pct_drop.argtypes = [vp, ci, C.POINTER(DropStats)]
     lib.pct_image_reconstruction.argtypes = [vp, C.POINTER(DropStats)]
+    lib.pct_drop_fp64.argtypes = [vp, ci, C.c_void_p, C.POINTER(DropStats)]
     lib.pct_get_counts.argtypes = [vp, C.POINTER(Counts)]
     lib.pct_get_array.argtypes = [vp, ci, vp, C.POINTER(C.c_size_t)]
     lib.pct_array_device_ptr.argtypes = [vp, ci, C.POINTER(vp), C.POINTER(C.c_size_t)]
@@ -181,6 +182,14 @@ class Reconstruction:
         st = DropStats()
         self._call("pct_drop", int(iterations), C.byref(st))
         return st
+
+    def drop_fp64(self, iterations, x):
+        """Binary64 DROP iterations from image x (NUM_VOXELS values, linear order); returns
+        (the binary64 image, stats).  The binary32 iterate is not touched (pct_drop_fp64)."""
+        xd = np.array(x, dtype=np.float64, copy=True)
+        st = DropStats()
+        self._call("pct_drop_fp64", int(iterations), C.c_void_p(xd.ctypes.data), C.byref(st))
+        return xd, st
 
     def image_reconstruction_GPU(self):
         st = DropStats()

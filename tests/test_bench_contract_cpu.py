@@ -1,5 +1,6 @@
 """bench.py's reference arm on the host (no GPU): one JSON line with the
-contract's keys, on a bounded sample of the cfg2 workload."""
+contract's keys, on one full DROP block of the cfg2 workload, without mapping
+the CUDA library."""
 import json
 import os
 import subprocess
@@ -29,3 +30,6 @@ def test_reference_arm_prints_one_contract_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # the arm runs the CPU restatement alone: no library of the product is mapped
+    assert d["libraries_mapped"] and all(p.startswith("oracle" + os.sep) for p in d["libraries_mapped"]), \
+        d["libraries_mapped"]

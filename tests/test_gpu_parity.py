@@ -182,6 +182,31 @@ def test_drop_within_tolerance_of_fp64(run):
     assert all(np.isfinite(st.residual[k]) and st.residual[k] > 0 for k in range(its))
 
 
+def test_drop_fp64_mode_matches_the_binary64_oracle(run):
+    """pct_drop_fp64 (binary64 chord, dot, update and iterate on the GPU) against the
+    oracle's binary64 DROP of the same iterations: they differ only in the order of
+    the binary64 update sums; and the binary32 iterate stays within 1e-4 of it."""
+    name, cfg, ora, out = run
+    its = cfg.iterations
+    if its == 0:
+        pytest.skip("no iterations")
+    w, _ = CASES[name]()
+    data, angles = phantoms.generate(w)
+    r = recon.run_full(cfg, data, angles)
+    r.collect_mlp_endpoints()
+    r.mlp_rows()
+    x0 = r.array("X0")
+    x64, st = r.drop_fp64(its, x0)
+    assert same(r.array("X"), x0), "pct_drop_fp64 changed the binary32 iterate"
+    r.close()
+    ref = ora["x_%d" % its]
+    err = np.linalg.norm(x64 - ref) / np.linalg.norm(ref)
+    assert err <= 1e-9, "binary64 GPU vs oracle: relative L2 %.3e" % err
+    err32 = np.linalg.norm(out["X"].astype(np.float64) - x64) / np.linalg.norm(x64)
+    assert err32 <= DROP_TOL, "binary32 vs binary64 GPU: relative L2 %.3e" % err32
+    assert st.iterations_run == its and all(st.residual[k] > 0 for k in range(its))
+
+
 @pytest.mark.parametrize("form", [1, 2])
 def test_drop_other_forms_within_tolerance(run, form):
     """The sorted (1) and tiled (2) forms of the DROP block step against the
