@@ -56,8 +56,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=60000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--drop-form", type=int, default=0, choices=[0, 1, 2],
-                    help="DROP block step: 0 scatter (default), 1 sorted, 2 tiled")
+    ap.add_argument("--drop-form", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="DROP block step: 0 scatter (default), 1 sorted, 2 tiled, 3 gather")
     ap.add_argument("--voxel-order", type=int, default=0, choices=[0, 1],
                     help="internal voxel order: 0 bricks where the grid allows (default), 1 linear")
     a = ap.parse_args()
@@ -345,8 +345,14 @@ def main():
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     drop_bytes = R * 24 + rows * 4
     achieved = drop_bytes / drop_iter_s / 1e9
+    # the gather form also streams its column lists (4 B per stored entry) and
+    # their slice offsets (8 B per 32 voxels per block) every iteration
+    list_entries = c1["drop_list_entries"]
+    nblocks = (R + cfg.block_size - 1) // cfg.block_size
+    stream_bytes = drop_bytes + (list_entries * 4 + nblocks * ((phantoms.geometry(cfg).num_voxels + 31) // 32) * 8
+                                 if list_entries else 0)
     forms = {0: "k_drop_rows + k_drop_relax (scatter)", 1: "k_drop_rows + k_drop_relax (sorted)",
-             2: "k_tile_fwd + k_tile_rows + k_tile_bwd (tiled)"}
+             2: "k_tile_fwd + k_tile_rows + k_tile_bwd (tiled)", 3: "k_gather_rows + k_gather_cols (gather)"}
     dom = "one DROP iteration: %s" % forms[a.drop_form]
     traffic = None
     tr = {}
@@ -496,7 +502,8 @@ def main():
                     "d2h_bytes_per_step": int(nv * 4), "seconds_per_step": e2e_t / a.e2e_steps},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "algorithmic_bytes": drop_bytes,
+                         "algorithmic_bytes": drop_bytes, "stream_bytes": stream_bytes,
+                         "column_list_entries": list_entries,
                          "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"},
             "roofline_l2": roofline_l2,
             "roofline_mlp": {"bound": "hbm", "kernel": "MLP row generation (k_mlp_bound .. k_mlp_dedupe)",

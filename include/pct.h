@@ -98,7 +98,7 @@ typedef struct pct_config {
     int mlp_exact;                 /* 1: every MLP sample in binary64 (slow path, for checks) */
     double mlp_face_margin;        /* [cm] binary32 MLP samples closer than this to a voxel face
                                       are recomputed in binary64 (default 2e-5) */
-    int drop_form;                 /* DROP block step: PCT_DROP_SCATTER (default), _SORTED or _TILED */
+    int drop_form;                 /* DROP block step: PCT_DROP_SCATTER (default), _SORTED, _TILED or _GATHER */
     int walk_exact;                /* 1: every hull-walk step in binary64 (slow path, for checks) */
     int voxel_order;               /* internal voxel order of the MLP rows and the DROP iterate:
                                       PCT_ORDER_AUTO (4x2x1 bricks when COLUMNS % 4 == 0 and ROWS % 2 == 0)
@@ -124,7 +124,7 @@ enum { PCT_ORDER_AUTO = 0, PCT_ORDER_LINEAR = 1 };
  * accumulates in shared memory with exact integer sums, so the iterate is
  * reproducible bit for bit (falls back to SCATTER when its memory is not
  * free). */
-enum { PCT_DROP_SCATTER = 0, PCT_DROP_SORTED = 1, PCT_DROP_TILED = 2 };
+enum { PCT_DROP_SCATTER = 0, PCT_DROP_SORTED = 1, PCT_DROP_TILED = 2, PCT_DROP_GATHER = 3 };
 
 /* Geometry derived from a pct_config, as the reference macros derive it. */
 typedef struct pct_geometry {
@@ -189,6 +189,7 @@ typedef struct pct_counts {
     int64_t mlp_fp64_samples;        /* MLP samples recomputed in FP64 near a voxel face */
     int64_t walk_fp64_steps;         /* hull-walk steps taken in FP64 (binary32 could not certify them) */
     int64_t kernel_launches;         /* kernels this context has launched (graph nodes included) */
+    int64_t drop_list_entries;       /* gather DROP form: stored column-list entries (padding included) */
 } pct_counts;
 
 /* Per-iteration DROP statistics (GB300 extension). */

@@ -363,8 +363,10 @@ static pct_status build_scatter(pct_ctx* c) {
     return PCT_OK;
 }
 
-/* Bin order of every block's rows for the sorted form (counts as in the scatter form). */
-static pct_status build_sorted(pct_ctx* c) {
+/* Bin order of every block's rows: drop_perm[start + j] is the block-local
+ * index of the block's j-th row in sinogram bin order (a counting sort per
+ * block, once per set of rows). */
+pct_status pct_drop_bin_order(pct_ctx* c) {
     const int64_t n = c->h.n;
     const uint32_t nkeys = (uint32_t)c->geo.num_bins;
     const int tiles = (int)((nkeys + SCAN_TILE - 1) / SCAN_TILE);
@@ -389,6 +391,12 @@ static pct_status build_sorted(pct_ctx* c) {
         k_sort_fill<<<pct_grid_for(e - s, 256), 256, 0, c->stream>>>(s, e, bin, nkeys, cnt, off, perm);
     }
     PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
+
+/* The sorted form: the scatter form visiting each block's rows in bin order. */
+static pct_status build_sorted(pct_ctx* c) {
+    PCT_TRY(pct_drop_bin_order(c));
     PCT_TRY(build_scatter(c));
     c->drop_mode = PCT_DROP_SORTED;
     return PCT_OK;
@@ -465,6 +473,10 @@ static void enqueue_iteration(pct_ctx* c, double* resid) {
             pct_drop_tiled_enqueue(c, k, resid);
             continue;
         }
+        if (c->drop_mode == PCT_DROP_GATHER) {
+            pct_drop_gather_enqueue(c, k, resid);
+            continue;
+        }
         enqueue_block_rows(c, k, resid);
         enqueue_block_relax(c, k);
     }
@@ -490,6 +502,7 @@ pct_status pct_drop_prepare(pct_ctx* c) {
     if (!c->diag_ready) {
         pct_drop_release_graph(c);
         c->td.release();
+        pct_drop_gather_release(c);
         const int form = c->cfg.drop_form;
         if (form == PCT_DROP_TILED && !c->allreduce && c->num_shards == 1 && pct_drop_tiled_fits(c)) {
             PCT_TRY(pct_drop_tiled_build(c));
@@ -503,6 +516,14 @@ pct_status pct_drop_prepare(pct_ctx* c) {
             c->diag_ready = 1;
         } else if (form == PCT_DROP_SORTED) {
             PCT_TRY(build_sorted(c));
+        } else if (form == PCT_DROP_GATHER && c->cfg.drop_variant == PCT_DROP_STANDARD && !c->allreduce &&
+                   c->num_shards == 1) {
+            /* the scatter form's per-block counts size the gather lists; without the
+             * memory for the lists the scatter form runs */
+            PCT_TRY(build_scatter(c));
+            const pct_status st = pct_drop_gather_build(c);
+            if (st == PCT_OK) c->drop_mode = PCT_DROP_GATHER;
+            else if (st != PCT_ERR_ALLOC) return st;
         } else {
             PCT_TRY(build_scatter(c));
         }

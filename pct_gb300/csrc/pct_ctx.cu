@@ -261,11 +261,11 @@ extern "C" pct_status pct_create(const pct_config* cfg, int device, pct_ctx** ou
     if (cfg->block_size <= 0) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: block_size must be positive");
     if (cfg->drop_variant < PCT_DROP_STANDARD || cfg->drop_variant > PCT_DROP_ROBUST2)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_variant %d", cfg->drop_variant);
-    if (cfg->drop_variant != PCT_DROP_STANDARD && cfg->drop_form == PCT_DROP_TILED)
+    if (cfg->drop_variant != PCT_DROP_STANDARD && (cfg->drop_form == PCT_DROP_TILED || cfg->drop_form == PCT_DROP_GATHER))
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: the DROP variants run in the scatter or sorted form");
     if (cfg->voxel_order != PCT_ORDER_AUTO && cfg->voxel_order != PCT_ORDER_LINEAR)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: voxel_order %d", cfg->voxel_order);
-    if (cfg->drop_form < PCT_DROP_SCATTER || cfg->drop_form > PCT_DROP_TILED)
+    if (cfg->drop_form < PCT_DROP_SCATTER || cfg->drop_form > PCT_DROP_GATHER)
         return pct_fail(PCT_ERR_ARGUMENT, "pct_create: drop_form %d", cfg->drop_form);
     if (cfg->mlp_hull < 0 || cfg->mlp_hull > 3) return pct_fail(PCT_ERR_ARGUMENT, "pct_create: bad mlp_hull");
     if (cfg->mlp_tabulated != 0 && cfg->mlp_tabulated != 1)
@@ -316,7 +316,9 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->rows, &c->chord, &c->row_scale, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
                      &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order, &c->walk_order, &c->mlp_tab_trig, &c->mlp_tab_depth,
                      &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm,
-                     &c->d64_x, &c->d64_upd, &c->d64_chord, &c->d64_res};
+                     &c->d64_x, &c->d64_upd, &c->d64_chord, &c->d64_res,
+                     &c->gather_meta, &c->gather_off, &c->gather_slot, &c->gather_lists, &c->gather_val,
+                     &c->gather_tmp, &c->gather_steps};
     for (DevBuf* b : all) b->release();
     c->td.release();
     for (auto& b : c->in13) b.release();
@@ -352,6 +354,7 @@ extern "C" pct_status pct_get_counts(pct_ctx* c, pct_counts* out) {
         PCT_TRY(st);
         out->row_entries = total;
     }
+    out->drop_list_entries = c->drop_mode == PCT_DROP_GATHER ? c->gather_entries : 0;
     out->walks_capped = (int64_t)f[ERR_WALK_CAPPED];
     out->mlp_fp64_samples = (int64_t)f[ERR_MLP_FP64];
     out->walk_fp64_steps = (int64_t)f[ERR_WALK_FP64];

@@ -154,6 +154,9 @@ struct pct_ctx {
     int64_t dense_total = 0;
     DevBuf drop_resid;
     DevBuf d64_x, d64_upd, d64_chord, d64_res;  /* binary64 DROP (pct_drop_fp64) */
+    /* gather DROP form: rank-ordered row data, slice offsets and slots, column lists, row values */
+    DevBuf gather_meta, gather_off, gather_slot, gather_lists, gather_val, gather_tmp, gather_steps;
+    int64_t gather_entries = 0;
     cudaGraphExec_t drop_graph_exec = nullptr;  /* one DROP iteration */
     int64_t row_capacity = 0;
     int num_blocks = 0;
@@ -209,6 +212,9 @@ enum { ERR_WALK_CAPPED = 0, ERR_VOXEL_OUTSIDE = 1, ERR_FIXED_OVERFLOW = 2, ERR_R
 
 DevGeom pct_make_devgeom(const pct_config& c, const pct_geometry& g);
 void pct_drop_release_graph(pct_ctx* c);
+void pct_drop_gather_release(pct_ctx* c);
+pct_status pct_drop_gather_build(pct_ctx* c);
+void pct_drop_gather_enqueue(pct_ctx* c, int block, double* resid);
 pct_status pct_scan_lengths(pct_ctx* c, const int64_t* len, int64_t n, int64_t* off, int64_t* total);
 pct_status pct_rows_dense(pct_ctx* c, int64_t* total, DevBuf* dense_off, DevBuf* dense);
 int pct_drop_tiled_fits(pct_ctx* c);

@@ -30,7 +30,8 @@ class Counts(C.Structure):
     _fields_ = [("total_histories", C.c_int64), ("recon_vol_histories", C.c_int64),
                 ("post_cut_histories", C.c_int64), ("reconstruction_histories", C.c_int64),
                 ("row_entries", C.c_int64), ("rows_outside_image", C.c_int64), ("walks_capped", C.c_int64),
-                ("mlp_fp64_samples", C.c_int64), ("walk_fp64_steps", C.c_int64), ("kernel_launches", C.c_int64)]
+                ("mlp_fp64_samples", C.c_int64), ("walk_fp64_steps", C.c_int64), ("kernel_launches", C.c_int64),
+                ("drop_list_entries", C.c_int64)]
 
 
 class DropStats(C.Structure):

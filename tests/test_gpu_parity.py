@@ -207,9 +207,9 @@ def test_drop_fp64_mode_matches_the_binary64_oracle(run):
     assert st.iterations_run == its and all(st.residual[k] > 0 for k in range(its))
 
 
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 def test_drop_other_forms_within_tolerance(run, form):
-    """The sorted (1) and tiled (2) forms of the DROP block step against the
+    """The sorted (1), tiled (2) and gather (3) forms of the DROP block step against the
     same binary64 iterate (the default scatter form is checked above); the form
     asked for is the one that ran."""
     name, cfg, ora, out = run
