@@ -55,3 +55,13 @@ def test_compat_layer_exports_the_reference_entry_points():
     assert not missing, missing
     for ref_name in ("read_data_chunk", "hull_detection", "calculate_means", "FBP", "image_reconstruction_GPU"):
         assert ref_name in exported
+
+
+def test_cnn_header_is_exported():
+    lib = _capi.load()
+    names = declared_functions("pct_cnn.h")
+    assert "pct_cnn_train_step" in names and "pct_cnn_warm_start" in names, names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.pct_cnn_num_params.restype = C.c_size_t
+    assert lib.pct_cnn_num_params() == 27 * (2 * 32 + 6 * 32 * 32 + 32) + 7 * 32 + 1
