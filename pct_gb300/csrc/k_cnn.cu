@@ -479,10 +479,10 @@ struct pct_cnn {
     int depth = 0, height = 0, device = 0;
     int64_t nv = 0;
     cudaStream_t stream = nullptr;
-    DevBuf in0, act[CNN_LAYERS - 1], out, dy8, dyb[2], x0, hull, target;
+    DevBuf in0, act[CNN_LAYERS - 1], out, dy8, dyl[CNN_LAYERS - 1], x0, hull, target;
     DevBuf params, grads, adam_m, adam_v, gpad, bgrad, loss, err, scratch;
     DevBuf wf[CNN_LAYERS], wt[CNN_LAYERS], bias[CNN_LAYERS];
-    CUtensorMap map_in0, map_act[CNN_LAYERS - 1], map_dy8, map_dyb[2], map_wf[CNN_LAYERS], map_wt[CNN_LAYERS];
+    CUtensorMap map_in0, map_act[CNN_LAYERS - 1], map_dy8, map_dyl[CNN_LAYERS - 1], map_wf[CNN_LAYERS], map_wt[CNN_LAYERS];
     int64_t woff[CNN_LAYERS], boff[CNN_LAYERS], nparams = 0;
     int adam_t = 0;
     int sms = 1;
@@ -581,7 +581,7 @@ pct_status forward(pct_cnn* n) {
 
 /* loss and every parameter's gradient (into n->grads) for the current input and
  * target; dY of layer l is the gradient at layer l's output before its ReLU:
- * layer 7 in dy8, layers 6, 5, ... alternately in dyb[0], dyb[1], ... */
+ * layer 7 in dy8, layer l < 7 in dyl[l] */
 pct_status backward(pct_cnn* n) {
     PCT_CUDA(cudaMemsetAsync(n->loss.p, 0, sizeof(double), n->stream));
     ++n->launches;
@@ -589,9 +589,8 @@ pct_status backward(pct_cnn* n) {
                                                   n->dy8.as<uint16_t>(), n->loss.as<double>());
     const int rows = n->depth * n->height;
     const int slabs = (rows + 31) / 32;
-    int cur = 0;
     for (int l = CNN_LAYERS - 1; l >= 0; --l) {
-        const uint16_t* dy = l == CNN_LAYERS - 1 ? n->dy8.as<uint16_t>() : n->dyb[cur].as<uint16_t>();
+        const uint16_t* dy = l == CNN_LAYERS - 1 ? n->dy8.as<uint16_t>() : n->dyl[l].as<uint16_t>();
         const int cin_p = LCIN[l], cout_p = LCOUT[l];
         PCT_CUDA(cudaMemsetAsync(n->gpad.p, 0, sizeof(float) * CNN_TAPS * cin_p * cout_p, n->stream));
         PCT_CUDA(cudaMemsetAsync(n->bgrad.p, 0, sizeof(float) * 32, n->stream));
@@ -616,15 +615,13 @@ pct_status backward(pct_cnn* n) {
         PCT_CUDA(cudaMemcpyAsync(n->grads.as<float>() + n->boff[l], n->bgrad.p, sizeof(float) * RCOUT[l],
                                  cudaMemcpyDeviceToDevice, n->stream));
         if (l > 0) { /* dY of layer l - 1 = (W_l^T conv dY_l) masked by layer l's input > 0 */
-            const int nxt = l == CNN_LAYERS - 1 ? 0 : 1 - cur;
             ConvArgs a = conv_args(n);
             a.mask = layer_input(n, l);
-            a.out_bf = n->dyb[nxt].as<uint16_t>();
+            a.out_bf = n->dyl[l - 1].as<uint16_t>();
             if (l == CNN_LAYERS - 1)
                 PCT_TRY((launch_conv<16, 32, EPI_DGRAD>(n, n->map_dy8, n->map_wt[l], a)));
             else
-                PCT_TRY((launch_conv<32, 32, EPI_DGRAD>(n, n->map_dyb[cur], n->map_wt[l], a)));
-            cur = nxt;
+                PCT_TRY((launch_conv<32, 32, EPI_DGRAD>(n, n->map_dyl[l], n->map_wt[l], a)));
         }
     }
     PCT_CUDA(cudaGetLastError());
@@ -684,14 +681,17 @@ extern "C" pct_status pct_cnn_destroy(pct_cnn* n) {
     if (!n) return PCT_OK;
     cudaSetDevice(n->device);
     if (n->stream) cudaStreamSynchronize(n->stream);
-    DevBuf* bufs[] = {&n->in0, &n->out, &n->dy8, &n->dyb[0], &n->dyb[1], &n->x0, &n->hull, &n->target, &n->params,
+    DevBuf* bufs[] = {&n->in0, &n->out, &n->dy8, &n->x0, &n->hull, &n->target, &n->params,
                       &n->grads, &n->adam_m, &n->adam_v, &n->gpad, &n->bgrad, &n->loss, &n->err, &n->scratch};
     for (DevBuf* b : bufs) b->release();
     for (int l = 0; l < CNN_LAYERS; ++l) {
         n->wf[l].release();
         n->wt[l].release();
         n->bias[l].release();
-        if (l < CNN_LAYERS - 1) n->act[l].release();
+        if (l < CNN_LAYERS - 1) {
+            n->act[l].release();
+            n->dyl[l].release();
+        }
     }
     if (n->stream) cudaStreamDestroy(n->stream);
     delete n;
@@ -733,8 +733,7 @@ extern "C" pct_status pct_cnn_create(int device, int depth, int height, int widt
     for (int l = 0; l < CNN_LAYERS - 1 && st == PCT_OK; ++l) st = n->act[l].alloc(nv * 32 * 2);
     if (st == PCT_OK) st = n->out.alloc(nv * 4);
     if (st == PCT_OK) st = n->dy8.alloc(nv * 16 * 2);
-    if (st == PCT_OK) st = n->dyb[0].alloc(nv * 32 * 2);
-    if (st == PCT_OK) st = n->dyb[1].alloc(nv * 32 * 2);
+    for (int l = 0; l < CNN_LAYERS - 1 && st == PCT_OK; ++l) st = n->dyl[l].alloc(nv * 32 * 2);
     if (st == PCT_OK) st = n->x0.alloc(nv * 4);
     if (st == PCT_OK) st = n->hull.alloc(nv);
     if (st == PCT_OK) st = n->target.alloc(nv * 4);
@@ -756,15 +755,14 @@ extern "C" pct_status pct_cnn_create(int device, int depth, int height, int widt
     if (cudaMemsetAsync(n->params.p, 0, P * 4, n->stream) != cudaSuccess ||
         cudaMemsetAsync(n->adam_m.p, 0, P * 4, n->stream) != cudaSuccess ||
         cudaMemsetAsync(n->adam_v.p, 0, P * 4, n->stream) != cudaSuccess ||
-        cudaMemsetAsync(n->err.p, 0, 8, n->stream) != cudaSuccess ||
-        cudaMemsetAsync(n->dyb[0].p, 0, nv * 64, n->stream) != cudaSuccess ||
-        cudaMemsetAsync(n->dyb[1].p, 0, nv * 64, n->stream) != cudaSuccess)
+        cudaMemsetAsync(n->err.p, 0, 8, n->stream) != cudaSuccess)
         return fail(pct_fail(PCT_ERR_CUDA, "pct_cnn_create: memset"));
     st = make_act_map(&n->map_in0, n->in0.p, 16, height, depth);
     for (int l = 0; l < CNN_LAYERS - 1 && st == PCT_OK; ++l)
         st = make_act_map(&n->map_act[l], n->act[l].p, 32, height, depth);
     if (st == PCT_OK) st = make_act_map(&n->map_dy8, n->dy8.p, 16, height, depth);
-    for (int k = 0; k < 2 && st == PCT_OK; ++k) st = make_act_map(&n->map_dyb[k], n->dyb[k].p, 32, height, depth);
+    for (int l = 0; l < CNN_LAYERS - 1 && st == PCT_OK; ++l)
+        st = make_act_map(&n->map_dyl[l], n->dyl[l].p, 32, height, depth);
     for (int l = 0; l < CNN_LAYERS && st == PCT_OK; ++l) {
         st = make_w_map(&n->map_wf[l], n->wf[l].p, LCIN[l], LCOUT[l]);
         if (st == PCT_OK && l > 0) st = make_w_map(&n->map_wt[l], n->wt[l].p, LCOUT[l], LCIN[l]);
@@ -869,7 +867,7 @@ extern "C" pct_status pct_cnn_inspect(pct_cnn* n, int kind, int layer, float* ho
         src = n->dy8.as<uint16_t>();
         C = 16;
     }
-    if (kind == 1 && layer >= 0 && layer < CNN_LAYERS - 1) src = n->dyb[(CNN_LAYERS - 2 - layer) & 1].as<uint16_t>();
+    if (kind == 1 && layer >= 0 && layer < CNN_LAYERS - 1) src = n->dyl[layer].as<uint16_t>();
     if (!src || !host || count != (size_t)n->nv * C) return pct_fail(PCT_ERR_ARGUMENT, "pct_cnn_inspect: bad request");
     k_bf_to_f<<<pct_grid_for(n->nv * C, 256), 256, 0, n->stream>>>(n->nv * C, src, n->scratch.as<float>());
     PCT_CUDA(cudaGetLastError());

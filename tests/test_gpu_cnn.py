@@ -102,7 +102,8 @@ def test_gradients_every_layer(setup):
     out = net.forward(x0, hull).reshape(D, H, W)
     loss, g = net.gradients(x0, hull, target)
     loss2, g2 = net.gradients(x0, hull, target)
-    assert np.array_equal(g, g2), "gradients differ between identical calls"
+    # the CTAs' partial sums meet in float atomics: identical calls agree to rounding
+    assert rel_l2(g2, g.astype(np.float64)) <= 1e-6, "gradients of identical calls differ"
     nv = D * H * W
     assert abs(loss - np.mean((out.astype(np.float64) - target) ** 2)) <= 1e-6 * max(loss, 1e-30)
     sl = cnn.param_slices()
