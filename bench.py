@@ -48,8 +48,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--histories", type=int, default=None,
                     help="scan size (default: 30M for cfg2, 60M for cfg4)")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg4"],
-                    help="cfg2 (the bench line: 256x256x32, 8-insert cylinder) or cfg4 (320x320x64 head phantom)")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg4", "cfg5"],
+                    help="cfg2 (the bench line: 256x256x32, 8-insert cylinder), cfg4 (320x320x64 head phantom) or "
+                         "cfg5 (learned warm start: train the CNN, compare FBP-start and learned-start DROP)")
+    ap.add_argument("--train-phantoms", type=int, default=64, help="cfg5: training phantoms")
+    ap.add_argument("--eval-phantoms", type=int, default=8, help="cfg5: held-out phantoms")
+    ap.add_argument("--train-steps", type=int, default=3000, help="cfg5: Adam steps")
     ap.add_argument("--chord-bf16", type=int, default=None, choices=[0, 1],
                     help="round chords to bfloat16 (default: the workload's setting; cfg4 uses bf16)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -262,9 +266,80 @@ def run_reference_arm(a, ws, rank):
     print(json.dumps(out))
 
 
+def run_warmstart(a, ws, rank):
+    """--workload cfg5: the learned warm start.  Trains the CNN on FBP -> 20-iteration-DROP pairs
+    of seeded ellipsoid phantoms (128 x 128 x 16 grid) with the library's tensor-core kernels,
+    then runs DROP from the FBP start and from the learned start on held-out phantoms.
+    `value` = mean over held-out phantoms of (FBP-start seconds / learned-start seconds) to reach
+    a voxel RSP RMSE at or below the lowest the FBP start reaches in 30 iterations; the line
+    also gives the region-mean targets and the residual stop."""
+    if rank != 0:
+        return
+    from pct_gb300 import warmstart
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    with Clocks(0) as clk:
+        res = warmstart.experiment(a.train_phantoms, range(1001, 1001 + a.eval_phantoms), steps=a.train_steps)
+    evaluated = len(res["eval_seeds"])
+    nv = warmstart.COLS * warmstart.COLS * warmstart.SLICES
+    real, padded = warmstart.conv_flops(nv)
+    tf = padded / res["forward_seconds"] / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    summary = {}
+    for target in ("voxel_rmse_at_plain_best", "0.5pct", "within_10pct_of_plain_best", "residual_stop"):
+        rows = res["per_seed"]
+        it = {st: [r["%s_%s_iterations" % (st, target)] for r in rows] for st in ("fbp", "learned")}
+        sec = {st: [r["%s_%s_seconds" % (st, target)] for r in rows] for st in ("fbp", "learned")}
+        both = [(f, l) for f, l in zip(sec["fbp"], sec["learned"]) if f is not None and l is not None and l > 0]
+        summary[target] = {"iterations": it, "seconds": sec,
+                           "mean_time_ratio_fbp_over_learned": float(np.mean([f / l for f, l in both])) if both else None,
+                           "reached": {st: sum(v is not None for v in it[st]) for st in it}}
+    rows = res["per_seed"]
+    start = {st: {"region_error_pct": float(np.mean([r[st]["region_error_pct"][0] for r in rows])),
+                  "voxel_rmse_pct": float(np.mean([r[st]["voxel_rmse_pct"][0] for r in rows]))}
+             for st in ("fbp", "learned")}
+    value = summary["voxel_rmse_at_plain_best"]["mean_time_ratio_fbp_over_learned"]
+    out = {"metric": "wall time to RSP RMSE target (the lowest voxel RMSE plain DROP reaches): FBP start / learned "
+                     "start", "value": value, "unit": "x",
+           "n_gpus": ws, "steps": res["steps"], "warmup": 0, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "bf16 (network), f32 (DROP)",
+           "data": "synthetic (seeded ellipsoid phantoms of the batched-scan generator)",
+           "config": {"workload": "cfg5: %d training (of %d seeds tried: targets where plain DROP diverged are "
+                                  "skipped) / %d of %d held-out phantoms (the same rule), 128x128x16, %d histories "
+                                  "each, DROP block %d, lambda %.2g, targets = 20 plain DROP iterations, %d Adam steps"
+                                  % (len(res["train_seeds"]), res["seeds_tried"], evaluated, a.eval_phantoms,
+                                     res["histories"],
+                                     res["block_size"], res["lambda"], res["steps"])},
+           "targets": summary, "start_error": start,
+           "training": {"pairs_seconds": res["pairs_seconds"], "train_seconds": res["train_seconds"],
+                        "seconds_per_step": res["train_seconds"] / res["steps"],
+                        "loss_first_50": float(np.mean(res["losses"][:50])),
+                        "loss_last_50": float(np.mean(res["losses"][-50:]))},
+           "network_forward": {"seconds": res["forward_seconds"], "voxels": nv, "flops_real": real,
+                               "flops_tensor_core": padded, "tflops": tf,
+                               "frac_of_bf16_peak": tf / peak,
+                               "note": "host-timed pct_cnn_forward on device-resident input and output (the "
+                                       "call returns after its stream finishes)"},
+           "per_seed_region_error_pct": {str(r["seed"]): {"fbp": r["fbp"]["region_error_pct"][:16],
+                                                          "learned": r["learned"]["region_error_pct"][:16]}
+                                         for r in rows},
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+
+
 def main():
     a = parse()
     ws, rank, local = dist_env()
+    if a.workload == "cfg5":
+        if a.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned warm start"}))
+            return
+        run_warmstart(a, ws, rank)
+        return
     if a.impl == "reference":
         run_reference_arm(a, ws, rank)
         return

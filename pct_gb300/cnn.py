@@ -90,6 +90,10 @@ class Net:
         self._call("pct_cnn_forward", x0.ctypes.data, hull.ctypes.data, out.ctypes.data, 0)
         return out
 
+    def forward_device(self, x0_ptr, hull_ptr, out_ptr):
+        """network(x0, hull) on device pointers (nv floats, nv bytes, nv floats)."""
+        self._call("pct_cnn_forward", C.c_void_p(x0_ptr), C.c_void_p(hull_ptr), C.c_void_p(out_ptr), 1)
+
     def gradients(self, x0, hull, target):
         x0, hull, t = self._in(x0, hull, target)
         g = np.empty(self.nparams, np.float32)
