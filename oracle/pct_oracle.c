@@ -1179,9 +1179,11 @@ int ora_drop_shard(const pct_config* cfg, int64_t n, const int64_t* offsets, con
  *              c lambda r / (||a||^2 + psi_j), psi_j = ((1 - x_j) eta) psi_sign,
  *              relaxation DROP_update (.cu:8044-8055);
  *   variant 2  DROP_blocks_robust2 / DROP_update_robust2 (.cu:7871-7901): the
- *              standard update, and per voxel ||A||_j = sum of c^2 over the block's
- *              entries; x_j += ||A||_j / (||A||_j + psi_j) * update_j / s_j with
- *              psi_j = psi_sign (1 - x_j) eta.
+ *              standard update, and per voxel ||A||_j = sum of c^2 over every
+ *              entry in voxel j of the blocks processed so far (the reference
+ *              allocates norm_Ai once per reconstruction, .cu:7448, and never
+ *              clears it); x_j += ||A||_j / (||A||_j + psi_j) * update_j / s_j
+ *              with psi_j = psi_sign (1 - x_j) eta.
  * variant 0 is ora_drop. */
 int ora_drop_variant(const pct_config* cfg, int64_t n, const int64_t* offsets, const uint32_t* rows,
                      const double* chord, const float* wepl, int iterations, int block_size, double lambda,
@@ -1229,7 +1231,6 @@ int ora_drop_variant(const pct_config* cfg, int64_t n, const int64_t* offsets, c
                         x[v] += (norm_a[v] / (norm_a[v] + psi)) * upd[v] / cnt[v];
                     }
                     upd[v] = 0.0;
-                    norm_a[v] = 0.0;
                     cnt[v] = 0;
                 }
         }

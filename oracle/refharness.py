@@ -55,6 +55,11 @@ def load(geometry):
     lib.pctref_chord_host.argtypes = [C.c_double, C.c_double]
     lib.pctref_chord_gpu.restype = C.c_double
     lib.pctref_chord_gpu.argtypes = [C.c_double, C.c_double]
+    lib.pctref_write_endpoints.argtypes = [C.c_char_p, C.c_char_p]
+    lib.pctref_mlp_tables.argtypes = [C.c_char_p]
+    lib.pctref_mlp_path_tab.argtypes = [C.c_void_p, C.c_void_p, C.c_uint, C.c_void_p, C.POINTER(C.c_float)]
+    lib.pctref_drop_cpu.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_int, C.c_float, C.c_double, C.c_int, C.c_void_p]
     return lib
 
 
@@ -78,6 +83,13 @@ def _child(geometry, kw, out_path):
     os.dup2(devnull, 1)
     rc = lib.pctref_run(C.byref(run))
     arrays = {}
+    if rc == 0 and kw.get("endpoints_file"):
+        # write_MLP_endpoints on the histories the run kept
+        d = os.path.dirname(out_path)
+        os.makedirs(os.path.join(d, "endpoints"), exist_ok=True)
+        if lib.pctref_write_endpoints((d + "/").encode(), b"endpoints") == 0:
+            with open(os.path.join(d, "endpoints", "MLP_endpoints_r=1.bin"), "rb") as f:
+                arrays["pin.MLP_endpoints_file"] = np.frombuffer(f.read(), np.uint8).copy()
     for i in range(lib.pctref_capture_count()):
         name = lib.pctref_capture_name(i).decode()
         nbytes = lib.pctref_capture_bytes(i)

@@ -129,3 +129,35 @@ class Net:
     def warm_start(self, reconstruction):
         """x0 and the iterate of a Reconstruction (after define_initial_iterate) := network(x0, hull)."""
         _capi.check(self.lib.pct_cnn_warm_start(reconstruction.h, self.h), "pct_cnn_warm_start")
+
+
+def _main():
+    """Runs the network on random data: `reps` forward passes and one gradient pass, with
+    their host-timed durations (a self-check of the tensor-core kernels and a profiling
+    target)."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--depth", type=int, default=16)
+    ap.add_argument("--height", type=int, default=128)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args()
+    rng = np.random.default_rng(0)
+    net = Net(a.depth, a.height, 128)
+    net.init(1)
+    x0 = rng.uniform(0, 1.5, net.nv).astype(np.float32)
+    hull = (x0 > 0.2).astype(np.uint8)
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        out = net.forward(x0, hull)
+    t_fwd = (time.perf_counter() - t0) / max(a.reps, 1)
+    t0 = time.perf_counter()
+    loss, g = net.gradients(x0, hull, 0.9 * x0)
+    t_grad = time.perf_counter() - t0
+    net.close()
+    print("forward %.3f ms, forward + gradients %.3f ms, loss %.6g, |out| %.6g, |grad| %.6g"
+          % (t_fwd * 1e3, t_grad * 1e3, loss, float(np.abs(out).sum()), float(np.abs(g).sum())))
+
+
+if __name__ == "__main__":
+    _main()

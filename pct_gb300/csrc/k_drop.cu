@@ -49,7 +49,8 @@ __global__ void k_block_counts(int64_t start, int64_t end, const int64_t* __rest
 /* VARIANT 0: block_update_GPU; 1: DROP_blocks_red (.cu:7998-8021), the entry's
  * update c lambda r / (||a||^2 + psi_j) with psi_j = ((1 - x_j) eta) psi_sign,
  * in binary32; 2: DROP_blocks_robust2 (.cu:7871-7885), the standard update (its
- * per-voxel sums of c^2 are fixed by the rows and counted once, k_block_norms). */
+ * per-voxel sums of c^2 per block are fixed by the rows and counted once,
+ * k_block_norms; DROP_update_robust2 adds them up as the blocks go by). */
 template <int VARIANT>
 __global__ void __launch_bounds__(DROP_THREADS) k_drop_rows(int64_t start, int64_t end,
                                                             const uint32_t* __restrict__ perm,
@@ -177,16 +178,22 @@ __global__ void k_block_norms(int64_t start, int64_t end, const int64_t* __restr
 }
 
 /* DROP_update_robust2 (.cu:7887-7901): x += ||A|| / (||A|| + psi) * x_update / s,
- * psi = psi_sign (1 - x) eta. */
+ * psi = psi_sign (1 - x) eta, in binary64 as the reference.  ||A||_j is the sum
+ * of c^2 over every entry in voxel j of all blocks processed since the
+ * reconstruction started: the reference allocates norm_Ai once (.cu:7448) and
+ * never clears it, so `acc` gains this block's sums before they are used. */
 __global__ void k_drop_relax_robust2(int nv, const uint32_t* __restrict__ cnt, const float* __restrict__ norm,
-                                     float* __restrict__ x, float* __restrict__ upd, float eta, float psi_sign) {
+                                     double* __restrict__ acc, float* __restrict__ x, float* __restrict__ upd,
+                                     double eta, double psi_sign) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv) return;
     uint32_t s = cnt[v];
     if (s > 0) {
-        float xv = x[v], na = norm[v];
-        float psi = psi_sign * (1.0f - xv) * eta;
-        x[v] = xv + (na / (na + psi)) * upd[v] / (float)s;
+        const double na = acc[v] + (double)norm[v];
+        acc[v] = na;
+        const float xv = x[v];
+        const double psi = psi_sign * (1.0 - (double)xv) * eta;
+        x[v] = (float)((double)xv + (na / (na + psi)) * (double)upd[v] / (double)s);
         upd[v] = 0.0f;
     }
 }
@@ -340,6 +347,8 @@ static pct_status build_scatter(pct_ctx* c) {
     if (c->cfg.drop_variant == PCT_DROP_ROBUST2) {
         PCT_TRY(c->block_norm.alloc(sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1)));
         PCT_CUDA(cudaMemsetAsync(c->block_norm.p, 0, sizeof(float) * (size_t)nv * (nb > 0 ? nb : 1), c->stream));
+        PCT_TRY(c->robust_norm.alloc(sizeof(double) * (size_t)nv));
+        PCT_CUDA(cudaMemsetAsync(c->robust_norm.p, 0, sizeof(double) * (size_t)nv, c->stream));
         for (int k = 0; k < nb; ++k) {
             int64_t s, e;
             pct_drop_block_range(c, k, &s, &e);
@@ -441,8 +450,8 @@ static void enqueue_block_relax(pct_ctx* c, int k) {
     const float eta = (float)c->cfg.eta, sgn = (float)c->cfg.psi_sign;
     if (c->cfg.drop_variant == PCT_DROP_ROBUST2)
         k_drop_relax_robust2<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(
-            nv, c->block_diag.as<uint32_t>() + (size_t)k * nv, c->block_norm.as<float>() + (size_t)k * nv, xi,
-            c->x_update.as<float>(), eta, sgn);
+            nv, c->block_diag.as<uint32_t>() + (size_t)k * nv, c->block_norm.as<float>() + (size_t)k * nv,
+            c->robust_norm.as<double>(), xi, c->x_update.as<float>(), c->cfg.eta, (double)c->cfg.psi_sign);
     else if (nv % 4 == 0)
         k_drop_relax4<<<pct_grid_for(nv / 4, 256), 256, 0, c->stream>>>(
             nv / 4, reinterpret_cast<const uint4*>(c->block_diag.as<uint32_t>() + (size_t)k * nv),

@@ -315,7 +315,7 @@ extern "C" pct_status pct_destroy(pct_ctx* c) {
                      &c->fbp_hull, &c->x_hull, &c->x_hull_filtered, &c->x0, &c->x, &c->x_update, &c->row_offsets,
                      &c->rows, &c->chord, &c->row_scale, &c->mlp_table, &c->block_diag, &c->block_diag_offsets,
                      &c->drop_resid, &c->mlp_bound, &c->mlp_rec, &c->mlp_queue, &c->mlp_fix_rows, &c->mlp_order, &c->walk_order, &c->mlp_tab_trig, &c->mlp_tab_depth,
-                     &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm,
+                     &c->drop_perm, &c->drop_sort, &c->x_brick, &c->block_norm, &c->robust_norm,
                      &c->d64_x, &c->d64_upd, &c->d64_chord, &c->d64_res,
                      &c->gather_meta, &c->gather_off, &c->gather_slot, &c->gather_lists, &c->gather_val,
                      &c->gather_tmp, &c->gather_steps};
@@ -451,6 +451,8 @@ extern "C" pct_status pct_set_image(pct_ctx* c, const float* x) {
     PCT_TRY(c->x0.alloc(n));
     PCT_CUDA(cudaMemcpyAsync(c->x.p, x, n, cudaMemcpyHostToDevice, c->stream));
     PCT_CUDA(cudaMemcpyAsync(c->x0.p, x, n, cudaMemcpyHostToDevice, c->stream));
+    if (c->robust_norm.p)
+        PCT_CUDA(cudaMemsetAsync(c->robust_norm.p, 0, sizeof(double) * c->geo.num_voxels, c->stream));
     PCT_CUDA(cudaStreamSynchronize(c->stream));
     return PCT_OK;
 }
@@ -561,5 +563,7 @@ extern "C" pct_status pct_reset_iterate(pct_ctx* c) {
     STAGE_ENTRY(c);
     if (!c->x0.p || !c->x.p) return pct_fail(PCT_ERR_STATE, "pct_reset_iterate: no initial iterate");
     PCT_CUDA(cudaMemcpyAsync(c->x.p, c->x0.p, sizeof(float) * c->geo.num_voxels, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->robust_norm.p) /* a new reconstruction: the robust variant's running sums restart */
+        PCT_CUDA(cudaMemsetAsync(c->robust_norm.p, 0, sizeof(double) * c->geo.num_voxels, c->stream));
     return PCT_OK;
 }

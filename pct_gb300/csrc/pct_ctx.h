@@ -149,6 +149,7 @@ struct pct_ctx {
     DevBuf mlp_tab_trig, mlp_tab_depth;                              /* tables of the tabulated MLP */
     DevBuf block_diag, block_diag_offsets;  /* per DROP block: voxel counts s_j */
     DevBuf block_norm;             /* per DROP block: sum of c^2 per voxel (robust variant) */
+    DevBuf robust_norm;            /* robust variant: running per-voxel sum of c^2 since the start (binary64) */
     DevBuf drop_perm, drop_sort;           /* per-block bin order of the rows, sort scratch */
     DevBuf dense_off, dense_rows;  /* CSR view of the rows for pct_get_array */
     int64_t dense_total = 0;

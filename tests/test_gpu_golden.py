@@ -130,7 +130,7 @@ def test_every_stage_equals_the_reference(golden):
     skip = {"x_final", "sinogram_pre", "mlp.chord"}
     bad, checked = [], 0
     for k in _digest_names(fx):
-        if k in skip or (k.startswith("x_") and k[2:].isdigit() and k != "x_0"):
+        if k in skip or k.startswith("pin.") or (k.startswith("x_") and k[2:].isdigit() and k != "x_0"):
             continue
         assert k in got, "stage %s not produced" % k
         want_dtype = str(fx["dtype:" + k])
