@@ -262,6 +262,21 @@ pct_status pct_drop(pct_ctx* ctx, int iterations, pct_drop_stats* stats);
  * the error of pct_drop against a binary64 run of the same iterations; needs
  * the scatter or sorted form and the standard update.  stats may be NULL. */
 pct_status pct_drop_fp64(pct_ctx* ctx, int iterations, double* x, pct_drop_stats* stats);
+/* DROP iterations of several scans in one persistent launch per iteration
+ * (no reference counterpart: the reference reconstructs one scan per run,
+ * src/pCT_Reconstruction_Data_Segments.cu:6795-6844).  `count` distinct
+ * contexts on one device, each after pct_mlp_rows, each with its own block
+ * size, in the scatter form with the standard update and unsharded.  The
+ * blocks of all scans form one queue of work items (rows of a block, or
+ * voxels of its relaxation) taken by the CTAs of a cooperative launch;
+ * within a scan the blocks run in order, as pct_drop runs them.  At most 64
+ * iterations per call.  stats: `count` entries or NULL; every scan's
+ * `seconds` is the device time of the whole batch. */
+pct_status pct_drop_many(pct_ctx* const* ctxs, int count, int iterations, pct_drop_stats* stats);
+/* The MLP rows packed back to back, returning to the device the slack of the
+ * per-history slots (sized by the MLP sample count); no reference
+ * counterpart.  The rows, their order and the DROP results are unchanged. */
+pct_status pct_compact_rows(pct_ctx* ctx);
 /* image_reconstruction_GPU (pCT_functions.h:237): endpoints, rows, all
  * cfg->iterations DROP iterations. */
 pct_status pct_image_reconstruction(pct_ctx* ctx, pct_drop_stats* stats);

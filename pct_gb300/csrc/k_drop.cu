@@ -540,25 +540,67 @@ pct_status pct_drop_prepare(pct_ctx* c) {
     return PCT_OK;
 }
 
-pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
+/* Everything a run of DROP iterations needs before the first one: the
+ * per-block structures, a zero x_update, the iterate in the rows' voxel order
+ * and the residual slots ([0, maxit): per-iteration squared residual, maxit:
+ * accumulator, maxit+1: ||b||^2). */
+pct_status pct_drop_begin(pct_ctx* c) {
     if (c->stage != ST_ROWS) return pct_fail(PCT_ERR_STATE, "drop needs MLP rows");
-    if (iterations < 0) return pct_fail(PCT_ERR_ARGUMENT, "drop: negative iteration count");
     const int nv = c->geo.num_voxels;
     PCT_TRY(pct_drop_prepare(c));
     PCT_TRY(c->x_update.alloc(sizeof(float) * nv));
     PCT_CUDA(cudaMemsetAsync(c->x_update.p, 0, sizeof(float) * nv, c->stream));
-    const bool brick = c->dg.brick && c->drop_mode != PCT_DROP_TILED;
-    if (brick) {
+    if (c->dg.brick && c->drop_mode != PCT_DROP_TILED) {
         PCT_TRY(c->x_brick.alloc(sizeof(float) * nv));
         ++c->launches;
         k_image_to_brick<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(c->dg, c->x.as<float>(), c->x_brick.as<float>());
     }
-    const int maxit = 64;
-    /* [0, maxit): per-iteration squared residual, maxit: accumulator, maxit+1: ||b||^2 */
-    PCT_TRY(c->drop_resid.alloc(sizeof(double) * (maxit + 2)));
+    PCT_TRY(c->drop_resid.alloc(sizeof(double) * (PCT_DROP_MAXIT + 2)));
     double* d_res = c->drop_resid.as<double>();
-    PCT_CUDA(cudaMemsetAsync(d_res, 0, sizeof(double) * (maxit + 2), c->stream));
-    if (c->h.n > 0) k_wepl_norm<<<304, 256, 0, c->stream>>>(c->h.n, c->h.wepl.as<float>(), d_res + maxit + 1);
+    PCT_CUDA(cudaMemsetAsync(d_res, 0, sizeof(double) * (PCT_DROP_MAXIT + 2), c->stream));
+    if (c->h.n > 0)
+        k_wepl_norm<<<304, 256, 0, c->stream>>>(c->h.n, c->h.wepl.as<float>(), d_res + PCT_DROP_MAXIT + 1);
+    PCT_CUDA(cudaGetLastError());
+    return PCT_OK;
+}
+
+/* After the iterations: the iterate back in linear order, and the stats of
+ * `done` iterations that took `ms` milliseconds. */
+pct_status pct_drop_end(pct_ctx* c, int done, float ms, pct_drop_stats* stats) {
+    const int nv = c->geo.num_voxels, maxit = PCT_DROP_MAXIT;
+    if (c->dg.brick && c->drop_mode != PCT_DROP_TILED) {
+        ++c->launches;
+        k_image_from_brick<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(c->dg, c->x_brick.as<float>(), c->x.as<float>());
+    }
+    PCT_CUDA(cudaGetLastError());
+    double res_host[PCT_DROP_MAXIT + 2];
+    PCT_CUDA(cudaMemcpyAsync(res_host, c->drop_resid.p, sizeof(double) * (maxit + 2), cudaMemcpyDeviceToHost,
+                             c->stream));
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations_run = done;
+        double b2 = res_host[maxit + 1];
+        for (int k = 0; k < done && k < maxit; ++k) stats->residual[k] = b2 > 0 ? sqrt(res_host[k] / b2) : 0.0;
+        stats->seconds = ms * 1e-3;
+        stats->drop_form = c->drop_mode;
+    }
+    return PCT_OK;
+}
+
+/* Copies the iteration's squared residual into slot `it` and clears the accumulator. */
+void pct_drop_store_resid(pct_ctx* c, int it) {
+    double* d_res = c->drop_resid.as<double>();
+    ++c->launches;
+    k_store_resid<<<1, 1, 0, c->stream>>>(d_res + PCT_DROP_MAXIT, d_res + (it < PCT_DROP_MAXIT ? it : PCT_DROP_MAXIT - 1));
+}
+
+pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
+    if (c->stage != ST_ROWS) return pct_fail(PCT_ERR_STATE, "drop needs MLP rows");
+    if (iterations < 0) return pct_fail(PCT_ERR_ARGUMENT, "drop: negative iteration count");
+    PCT_TRY(pct_drop_begin(c));
+    const int maxit = PCT_DROP_MAXIT;
+    double* d_res = c->drop_resid.as<double>();
     PCT_TRY(drop_allreduce(c, d_res + maxit + 1, 1, PCT_DT_F64));
     if (!c->allreduce) PCT_TRY(capture_iteration(c, d_res + maxit));
     cudaEvent_t e0, e1;
@@ -574,8 +616,7 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
             PCT_CUDA(cudaGraphLaunch(c->drop_graph_exec, c->stream));
             c->launches += c->drop_launches_per_iter;
         }
-        ++c->launches;
-        k_store_resid<<<1, 1, 0, c->stream>>>(d_res + maxit, d_res + (it < maxit ? it : maxit - 1));
+        pct_drop_store_resid(c, it);
         ++done;
         if (c->cfg.residual_tol > 0.0) {
             PCT_CUDA(cudaMemcpyAsync(res_host, d_res, sizeof(double) * (maxit + 2), cudaMemcpyDeviceToHost, c->stream));
@@ -586,26 +627,12 @@ pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats) {
         }
     }
     PCT_CUDA(cudaEventRecord(e1, c->stream));
-    if (brick) {
-        ++c->launches;
-        k_image_from_brick<<<pct_grid_for(nv, 256), 256, 0, c->stream>>>(c->dg, c->x_brick.as<float>(), c->x.as<float>());
-    }
-    PCT_CUDA(cudaGetLastError());
-    PCT_CUDA(cudaMemcpyAsync(res_host, d_res, sizeof(double) * (maxit + 2), cudaMemcpyDeviceToHost, c->stream));
-    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    PCT_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (stats) {
-        memset(stats, 0, sizeof(*stats));
-        stats->iterations_run = done;
-        double b2 = res_host[maxit + 1];
-        for (int k = 0; k < done && k < maxit; ++k) stats->residual[k] = b2 > 0 ? sqrt(res_host[k] / b2) : 0.0;
-        stats->seconds = ms * 1e-3;
-        stats->drop_form = c->drop_mode;
-    }
-    return PCT_OK;
+    return pct_drop_end(c, done, ms, stats);
 }
 
 void pct_drop_release_graph(pct_ctx* c) {

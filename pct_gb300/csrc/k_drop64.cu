@@ -15,7 +15,7 @@
 #include <cstring>
 #include "pct_device.cuh"
 
-pct_status pct_drop_prepare(pct_ctx* c);                                    /* k_drop.cu */
+
 int pct_drop_num_blocks(const pct_ctx* c);                                  /* k_drop.cu */
 void pct_drop_block_range(const pct_ctx* c, int k, int64_t* s, int64_t* e); /* k_drop.cu */
 pct_status pct_row_chords64(pct_ctx* c, double* out);                       /* k_mlp.cu */

@@ -21,6 +21,7 @@
  *                 k_row_norms does both for rows read from a file.
  */
 #include <cuda_bf16.h>
+#include <utility>
 #include "pct_device.cuh"
 
 namespace {
@@ -1073,6 +1074,19 @@ __global__ void __launch_bounds__(256) k_mlp_dedupe(int64_t rows_cap, const int6
     }
 }
 
+/* Copies each row from its bounded slot to back-to-back storage, one warp per row. */
+__global__ void k_copy_rows(int64_t n, const int64_t* __restrict__ src_off, const int* __restrict__ len,
+                            const int64_t* __restrict__ dst_off, const uint32_t* __restrict__ src,
+                            uint32_t* __restrict__ dst) {
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const uint32_t* s = src + src_off[i];
+    uint32_t* d = dst + dst_off[i];
+    const int m = len[i];
+    for (int j = lane; j < m; j += 32) d[j] = s[j];
+}
+
 /* Dense copy of the bounded rows (for pct_get_array). */
 __global__ void k_pack_rows(DevGeom g, int64_t n, const int64_t* __restrict__ start, const int* __restrict__ len,
                             const int64_t* __restrict__ dense_off, const uint32_t* __restrict__ rows,
@@ -1327,6 +1341,56 @@ pct_status pct_stage_mlp_rows(pct_ctx* c) {
     c->diag_ready = 0;
     pct_drop_release_graph(c);
     c->stage = ST_ROWS;
+    return PCT_OK;
+}
+
+/* The rows packed back to back in the rows' voxel order: the slack of the
+ * bounded slots (one slot entry per MLP sample) and the MLP pass's per-history
+ * scratch are returned to the device.
+ * An extension of the reconstruction sequence with no reference counterpart:
+ * it lets many scans' rows stay resident together (pct_drop_many). */
+extern "C" pct_status pct_compact_rows(pct_ctx* c) {
+    if (!c) return pct_fail(PCT_ERR_ARGUMENT, "pct_compact_rows: null context");
+    PCT_TRY(c->set_device());
+    if (c->stage < ST_ROWS) return pct_fail(PCT_ERR_STATE, "pct_compact_rows needs the MLP rows");
+    const int64_t n = c->h.n;
+    if (n == 0) return PCT_OK;
+    DevBuf off, len64, dense;
+    int64_t total = 0;
+    PCT_TRY(off.alloc(sizeof(int64_t) * (n + 1)));
+    pct_status st = len64.alloc(sizeof(int64_t) * n);
+    if (st != PCT_OK) {
+        off.release();
+        return st;
+    }
+    ++c->launches;
+    k_len64<<<pct_grid_for(n, 256), 256, 0, c->stream>>>(n, c->row_len.as<int>(), len64.as<int64_t>());
+    st = pct_scan_lengths(c, len64.as<int64_t>(), n, off.as<int64_t>(), &total);
+    len64.release();
+    if (st == PCT_OK && total < c->row_capacity) st = dense.alloc(sizeof(uint32_t) * (total > 0 ? total : 1));
+    if (st != PCT_OK || total >= c->row_capacity) { /* failed, or no slack to return */
+        off.release();
+        return st;
+    }
+    ++c->launches;
+    k_copy_rows<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(
+        n, c->row_offsets.as<int64_t>(), c->row_len.as<int>(), off.as<int64_t>(), c->rows.as<uint32_t>(),
+        dense.as<uint32_t>());
+    PCT_CUDA(cudaGetLastError());
+    PCT_CUDA(cudaStreamSynchronize(c->stream));
+    std::swap(c->rows, dense);
+    std::swap(c->row_offsets, off);
+    dense.release();
+    off.release();
+    /* the MLP pass's scratch goes too (pct_mlp_rows allocates it again) */
+    c->mlp_bound.release();
+    c->mlp_rec.release();
+    c->mlp_queue.release();
+    c->mlp_fix_rows.release();
+    c->mlp_order.release();
+    c->row_capacity = total;
+    c->diag_ready = 0; /* the per-block structures hold row positions */
+    pct_drop_release_graph(c);
     return PCT_OK;
 }
 

@@ -548,6 +548,9 @@ extern "C" pct_status pct_set_block_size(pct_ctx* c, int block_size) {
         c->cfg.block_size = block_size;
         c->diag_ready = 0;
         pct_drop_release_graph(c);
+        /* sized by the block count: rebuilt for the new size */
+        c->block_diag.release();
+        c->block_norm.release();
     }
     return PCT_OK;
 }

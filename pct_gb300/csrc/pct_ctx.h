@@ -199,6 +199,12 @@ pct_status pct_stage_endpoints(pct_ctx* c);
 pct_status pct_stage_mlp_rows(pct_ctx* c);
 pct_status pct_stage_mlp_rows_tab(pct_ctx* c);
 pct_status pct_stage_drop(pct_ctx* c, int iterations, pct_drop_stats* stats);
+/* Iterations whose residual is kept (pct_drop_stats.residual). */
+constexpr int PCT_DROP_MAXIT = 64;
+pct_status pct_drop_prepare(pct_ctx* c);
+pct_status pct_drop_begin(pct_ctx* c);
+pct_status pct_drop_end(pct_ctx* c, int done, float ms, pct_drop_stats* stats);
+void pct_drop_store_resid(pct_ctx* c, int it);
 
 /* Stable compaction of src[src_off, src_off+n) by a keep flag into dst at dst_off. */
 pct_status pct_compact(pct_ctx* c, HistoryStore& src, int64_t src_off, int64_t n, const uint8_t* d_keep,

@@ -80,6 +80,8 @@ def _declare(lib):
     lib.pct_set_allreduce.argtypes = [vp, _capi.ALLREDUCE_FN, vp]
     lib.pct_memcpy.argtypes = [vp, vp, i64]
     lib.pct_set_block_size.argtypes = [vp, ci]
+    lib.pct_drop_many.argtypes = [C.POINTER(vp), ci, ci, C.POINTER(DropStats)]
+    lib.pct_compact_rows.argtypes = [vp]
 
 
 class Reconstruction:
@@ -184,6 +186,10 @@ class Reconstruction:
         self._call("pct_drop", int(iterations), C.byref(st))
         return st
 
+    def compact_rows(self):
+        """Packs the MLP rows back to back (pct_compact_rows)."""
+        self._call("pct_compact_rows")
+
     def drop_fp64(self, iterations, x):
         """Binary64 DROP iterations from image x (NUM_VOXELS values, linear order); returns
         (the binary64 image, stats).  The binary32 iterate is not touched (pct_drop_fp64)."""
@@ -242,6 +248,20 @@ class Reconstruction:
 
     def stream(self):
         return self.lib.pct_stream(self.h)
+
+
+def drop_many(recons, iterations):
+    """DROP iterations of several reconstructions (each after mlp_rows, with its
+    own block size) in one persistent launch per iteration (pct_drop_many);
+    returns their DropStats."""
+    recons = list(recons)
+    if not recons:
+        return []
+    lib = recons[0].lib
+    handles = (C.c_void_p * len(recons))(*[r.h for r in recons])
+    stats = (DropStats * len(recons))()
+    _capi.check(lib.pct_drop_many(handles, len(recons), int(iterations), stats), "pct_drop_many")
+    return list(stats)
 
 
 def run_full(config, data13, projection_angle, chunk=None, device=0):
