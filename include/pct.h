@@ -308,8 +308,7 @@ void* pct_stream(pct_ctx* ctx);
  * a static device array of PCT_NOALLOC_MAX_VOXELS voxels: larger images are
  * rejected with PCT_ERR_ARGUMENT.  Calls that overlap on one device share that
  * scratch and race.  The first call on a device (or pct_noalloc_setup() with
- * that device current) looks the scratch up and may load the module, so make
- * it before any stream capture. */
+ * that device current) looks the scratch up and may load the module. */
 #define PCT_NOALLOC_MAX_VOXELS (1 << 21)
 pct_status pct_noalloc_setup(void);
 pct_status pct_drop_noalloc(int64_t n, const int64_t* row_offsets, const uint32_t* rows, const float* chord,

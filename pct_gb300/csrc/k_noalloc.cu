@@ -4,17 +4,17 @@
  *
  * Who needs it: a caller whose process may not allocate at this point, for
  * example one that runs on a pre-sized memory pool with the CUDA allocator
- * locked, or one that records the call into its own stream sequence and must
- * not trigger cudaMalloc/cudaFree (which synchronise the device) in the middle
- * of it.  pct_drop() keeps its scratch in the context and may (re)allocate it;
- * this entry point needs no context at all.
+ * locked, or one that must not let cudaMalloc/cudaFree (which synchronise the
+ * device) run in the middle of its own sequence of work on a stream.
+ * pct_drop() keeps its scratch in the context and may (re)allocate it; this
+ * entry point needs no context at all.
  *
  * Scratch: the per-voxel update sums and the per-voxel row counts s_j of the
  * current block live in one file-scope __device__ array sized for
  * PCT_NOALLOC_MAX_VOXELS voxels (2 x 4 bytes per voxel, 16 MiB in all).  Its
  * address is looked up once per device with cudaGetSymbolAddress (that lookup
- * can load the module, so the first call on a device, or
- * pct_noalloc_setup(), should come before any stream capture).  There is one
+ * can load the module; pct_noalloc_setup() does it ahead of the first call).
+ * There is one
  * scratch per device: two calls that overlap on one device (different
  * streams or host threads) race on it and give wrong images.
  *

@@ -4,7 +4,8 @@ Collected last so that it also runs after every other GPU test has used the
 device; it builds its own context and runs on its own in a fresh process too.
 Two calls in a row on the same rows must each reproduce pct_drop's image and
 sweep residuals within the DROP tolerance (binary32 scatter-add order differs
-between runs).
+between runs), and the device's free memory must be the same before and after
+a call (after pct_noalloc_setup and a first call).
 """
 import ctypes as C
 
@@ -55,13 +56,20 @@ def test_noalloc_matches_pct_drop_on_two_calls(ctx):
     ptr = {k: r.device_ptr(k)[0] for k in ("ROW_OFFSETS", "ROWS", "CHORD", "H_WEPL", "X")}
     nv = phantoms.geometry(cfg).num_voxels
     resid = torch.zeros(ITERATIONS, dtype=torch.float64, device="cuda")
+    _capi.check(lib.pct_noalloc_setup(), "pct_noalloc_setup")
     torch.cuda.synchronize()
     for call in range(2):
         r.reset_iterate()
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         s = lib.pct_drop_noalloc(n, ptr["ROW_OFFSETS"], ptr["ROWS"], ptr["CHORD"], ptr["H_WEPL"], nv,
                                  cfg.block_size, cfg.lambda_, ITERATIONS, ptr["X"], resid.data_ptr(), r.stream())
         _capi.check(s, "pct_drop_noalloc")
-        x = r.array("X").astype(np.float64)   # synchronises the context stream
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
+        if call == 1:  # the first call may still load the module
+            assert free_after == free_before, "device free memory %d -> %d" % (free_before, free_after)
+        x = r.array("X").astype(np.float64)
         err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
         assert err <= TOL, "call %d: relative L2 %.3e" % (call, err)
         rel = np.sqrt(resid.cpu().numpy() / b2)
