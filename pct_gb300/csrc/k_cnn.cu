@@ -27,8 +27,15 @@
  *       fp32 (last layer), gradient masked by the layer input's ReLU (input
  *       gradients: the same convolution on dY with the taps mirrored and
  *       c_in / c_out exchanged).
- *   k_conv_wgrad           weight gradients dW[tap][co][ci] = sum_v dY[v][co]
- *       X[v + tap][ci] on the CUDA cores (fp32 FMA), one CTA per (tap, slab).
+ *   k_conv_wgrad<CIN, COUT>  weight gradients dW[tap][co][ci] = sum_v
+ *       X[v + tap][ci] dY[v][co] with tcgen05.mma as well: D[(tap, ci), co] =
+ *       A x B^T with A = the shifted inputs (rows (tap, ci), K = voxels) and
+ *       B = dY (rows co, K = voxels), both K-major from channel-major copies
+ *       (k_wg_shift holds one copy per x shift, so that every TMA box starts
+ *       on an aligned x); per 32-voxel chunk the 27 taps' boxes and dY's box
+ *       fill a stage, 128 / CIN taps make one M = 128 tile, and the 7 (or 4)
+ *       tiles accumulate in TMEM over the CTA's chunks; the epilogue adds the
+ *       CTA's partial sums to dW with fp32 atomics.
  *   k_adam, k_publish      Adam on the fp32 master weights, then the bf16
  *       copies in both tap orders.
  */
@@ -357,55 +364,188 @@ __global__ void k_cnn_loss(int64_t nv, const float* __restrict__ out, const floa
     }
 }
 
-/* dW[tap][co][ci] += sum over the slab's rows of dY[v][co] X[v + tap][ci]
- * (X zero outside the volume); fp32 on the CUDA cores.  One CTA per (tap, slab
- * of rows); each thread owns (COUT * CIN) / 256 outputs. */
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(256) k_conv_wgrad(int depth, int height, int rows_per_slab,
-                                                    const uint16_t* __restrict__ x, const uint16_t* __restrict__ dy,
-                                                    float* __restrict__ dw) {
-    __shared__ float sx[CNN_W][CIN + 1];
-    __shared__ float sd[CNN_W][COUT + 1];
-    const int tap = blockIdx.x % CNN_TAPS, slab = blockIdx.x / CNN_TAPS;
-    const int dz = tap / 9 - 1, dyy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    constexpr int PER = (CIN * COUT + 255) / 256;
-    float acc[PER];
+/* Channel-major copies of a layer input for the weight gradients:
+ * xs[d][c][v] = X[v with x shifted by d - 1][c] (0 outside the volume), d = 0, 1, 2;
+ * v = (z * height + y) * 128 + x. */
+template <int C>
+__global__ void k_wg_shift(int64_t nv, const uint16_t* __restrict__ x, uint16_t* __restrict__ xs) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int xx = (int)(i & (CNN_W - 1));
+    const int64_t row = i - xx;
 #pragma unroll
-    for (int k = 0; k < PER; ++k) acc[k] = 0.0f;
-    const int nrows = depth * height;
-    const int r0 = slab * rows_per_slab, r1 = r0 + rows_per_slab < nrows ? r0 + rows_per_slab : nrows;
-    for (int r = r0; r < r1; ++r) {
-        const int z = r / height, y = r - z * height;
-        const int zs = z + dz, ys = y + dyy;
-        const bool row_in = zs >= 0 && zs < depth && ys >= 0 && ys < height;
-        __syncthreads();
-        for (int i = threadIdx.x; i < CNN_W * CIN; i += 256) {
-            const int xv = i / CIN, c = i - xv * CIN, xs = xv + dx;
-            float val = 0.0f;
-            if (row_in && xs >= 0 && xs < CNN_W) val = bf(x[(((size_t)zs * height + ys) * CNN_W + xs) * CIN + c]);
-            sx[xv][c] = val;
-        }
-        for (int i = threadIdx.x; i < CNN_W * COUT; i += 256) {
-            const int xv = i / COUT, c = i - xv * COUT;
-            sd[xv][c] = bf(dy[(((size_t)z * height + y) * CNN_W + xv) * COUT + c]);
-        }
-        __syncthreads();
-        if (!row_in) continue;
+    for (int d = 0; d < 3; ++d) {
+        const int src = xx + d - 1;
+        uint32_t w[C / 2];
+        if (src >= 0 && src < CNN_W) {
+            const uint4* p = reinterpret_cast<const uint4*>(x + (row + src) * C);
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int o = threadIdx.x + 256 * k;
-            if (o < CIN * COUT) {
-                const int co = o / CIN, ci = o - co * CIN;
-                float a = acc[k];
-                for (int xv = 0; xv < CNN_W; ++xv) a = fmaf(sd[xv][co], sx[xv][ci], a);
-                acc[k] = a;
+            for (int k = 0; k < C / 8; ++k) {
+                const uint4 u = p[k];
+                w[4 * k] = u.x;
+                w[4 * k + 1] = u.y;
+                w[4 * k + 2] = u.z;
+                w[4 * k + 3] = u.w;
             }
+        } else {
+#pragma unroll
+            for (int k = 0; k < C / 2; ++k) w[k] = 0u;
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            xs[((int64_t)d * C + c) * nv + i] = (uint16_t)((c & 1) ? (w[c / 2] >> 16) : (w[c / 2] & 0xffffu));
+    }
+}
+
+/* dt[c][v] = dY[v][c] */
+template <int C>
+__global__ void k_wg_dyt(int64_t nv, const uint16_t* __restrict__ dy, uint16_t* __restrict__ dt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const uint4* p = reinterpret_cast<const uint4*>(dy + i * C);
+#pragma unroll
+    for (int k = 0; k < C / 8; ++k) {
+        const uint4 u = p[k];
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            dt[(int64_t)(8 * k + 2 * h) * nv + i] = (uint16_t)(w[h] & 0xffffu);
+            dt[(int64_t)(8 * k + 2 * h + 1) * nv + i] = (uint16_t)(w[h] >> 16);
         }
     }
+}
+
+constexpr int WG_STAGES = 3;
+constexpr int WG_CHUNK = 32; /* voxels of one x row per chunk: K of the stage (64-byte rows) */
+
+template <int CIN, int COUT>
+struct WgSmem {
+    static constexpr int TPT = 128 / CIN;                      /* taps per M = 128 tile */
+    static constexpr int MT = (CNN_TAPS + TPT - 1) / TPT;      /* tiles: 7 (CIN 32) or 4 (CIN 16) */
+    static constexpr int A_BOX = CIN * WG_CHUNK * 2;           /* one tap: CIN rows of 64 bytes */
+    static constexpr int A_TILE = 128 * WG_CHUNK * 2;          /* 8 KB */
+    static constexpr int A_BYTES = MT * A_TILE;                /* the last tile's missing taps: zeros */
+    static constexpr int B_BYTES = COUT * WG_CHUNK * 2;
+    static constexpr int STAGE = A_BYTES + ((B_BYTES + 1023) / 1024) * 1024;
+    static constexpr int OFF_BAR = WG_STAGES * STAGE + 8192;
+    static constexpr int NBAR = 2 * WG_STAGES + 1; /* full, empty, tmem full */
+    static constexpr int TOTAL = OFF_BAR + NBAR * 8 + 16 + 1024;
+    static constexpr int NCOL = MT * COUT;
+    static constexpr uint32_t TCOLS = NCOL <= 32 ? 32u : NCOL <= 64 ? 64u : NCOL <= 128 ? 128u : 256u;
+};
+
+struct WgArgs {
+    int height, chunks, per; /* 4 chunks per x row; this CTA: chunks [blockIdx.x * per, + per) */
+    float* dw;               /* [tap][COUT][CIN] fp32, accumulated */
+    unsigned long long* err;
+};
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(CONV_THREADS, 1) k_conv_wgrad(const __grid_constant__ CUtensorMap xs_map,
+                                                               const __grid_constant__ CUtensorMap dt_map, WgArgs p) {
+    using L = WgSmem<CIN, COUT>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
+    uint64_t* empty = full + WG_STAGES;
+    uint64_t* tfull = empty + WG_STAGES;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tfull + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = blockIdx.x * p.per;
+    const int c1 = c0 + p.per < p.chunks ? c0 + p.per : p.chunks;
+    /* the missing taps of the last tile read zeros */
+    constexpr int PAD = L::A_BYTES - CNN_TAPS * L::A_BOX;
+    for (int st = 0; st < WG_STAGES; ++st)
+        for (int k = threadIdx.x; k < PAD / 16; k += CONV_THREADS)
+            reinterpret_cast<uint4*>(smem + st * L::STAGE + CNN_TAPS * L::A_BOX)[k] = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < WG_STAGES; ++st) {
+            mbar_init(full + st, 1);
+            mbar_init(empty + st, 1);
+        }
+        mbar_init(tfull, 1);
+        mbar_fence_init();
+    }
+    if (warp == 0) tmem_alloc(tslot, L::TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    bool ok = c1 > c0;
+    if (warp == 0) {
+        if (lane == 0 && ok) { /* TMA producer */
+            uint32_t it = 0;
+            for (int c = c0; c < c1; ++c, ++it) {
+                const int st = (int)(it % WG_STAGES);
+                const uint32_t round = it / WG_STAGES;
+                if (round > 0 && !mbar_wait(empty + st, (round - 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* sa = smem + st * L::STAGE;
+                uint8_t* sb = sa + L::A_BYTES;
+                const int row = c >> 2, x0 = (c & 3) * WG_CHUNK;
+                const int z = row / p.height, y = row - z * p.height;
+                mbar_expect_tx(full + st, (uint32_t)(CNN_TAPS * L::A_BOX + L::B_BYTES));
+                for (int tap = 0; tap < CNN_TAPS; ++tap) {
+                    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+                    tma_load_4d(sa + tap * L::A_BOX, &xs_map, x0, y + dy, z + dz, (dx + 1) * CIN, full + st);
+                }
+                tma_load_4d(sb, &dt_map, x0, y, z, 0, full + st);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && ok) { /* MMA issuer */
+            constexpr uint32_t idesc = umma_idesc(COUT);
+            uint32_t it = 0;
+            for (int c = c0; c < c1; ++c, ++it) {
+                const int st = (int)(it % WG_STAGES);
+                if (!mbar_wait(full + st, (it / WG_STAGES) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = saddr(smem + st * L::STAGE), b0 = a0 + L::A_BYTES;
 #pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int o = threadIdx.x + 256 * k;
-        if (o < CIN * COUT) atomicAdd(dw + (size_t)tap * CIN * COUT + o, acc[k]);
+                for (int m = 0; m < L::MT; ++m)
+#pragma unroll
+                    for (int kk = 0; kk < WG_CHUNK / 16; ++kk)
+                        umma_bf16(tmem + (uint32_t)(m * COUT), umma_desc(a0 + m * L::A_TILE + kk * 32, 64),
+                                  umma_desc(b0 + kk * 32, 64), idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                umma_commit(empty + st); /* the stage is free once these MMAs have read it */
+            }
+            if (ok) umma_commit(tfull);
+        }
+    } else if (ok) { /* epilogue: warps 2-5, TMEM lanes 32 * (warp % 4) .. + 31 */
+        const int q = warp & 3;
+        const int r = q * 32 + lane; /* D row: (tap within the tile, c_in) */
+        const int tl = r / CIN, ci = r - tl * CIN;
+        if (!mbar_wait(tfull, 0)) {
+            ok = false;
+        } else {
+            tc_fence_after();
+#pragma unroll 1
+            for (int m = 0; m < L::MT; ++m) {
+                uint32_t v[32];
+                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(m * COUT), v);
+                if (COUT > 16) tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(m * COUT) + 16, v + 16);
+                tmem_wait_ld();
+                const int tap = m * L::TPT + tl;
+                if (tap < CNN_TAPS)
+#pragma unroll
+                    for (int co = 0; co < COUT; ++co)
+                        atomicAdd(p.dw + ((size_t)tap * COUT + co) * CIN + ci, __uint_as_float(v[co]));
+            }
+            tc_fence_before();
+        }
+    }
+    if (!ok && c1 > c0 && lane == 0 && warp < 6) atomicAdd(p.err, 1ull);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L::TCOLS);
     }
 }
 
@@ -481,8 +621,10 @@ struct pct_cnn {
     cudaStream_t stream = nullptr;
     DevBuf in0, act[CNN_LAYERS - 1], out, dy8, dyl[CNN_LAYERS - 1], x0, hull, target;
     DevBuf params, grads, adam_m, adam_v, gpad, bgrad, loss, err, scratch;
+    DevBuf wg_x, wg_dy; /* channel-major copies for the weight gradients */
     DevBuf wf[CNN_LAYERS], wt[CNN_LAYERS], bias[CNN_LAYERS];
     CUtensorMap map_in0, map_act[CNN_LAYERS - 1], map_dy8, map_dyl[CNN_LAYERS - 1], map_wf[CNN_LAYERS], map_wt[CNN_LAYERS];
+    CUtensorMap map_xs16, map_xs32, map_dt16, map_dt32; /* over wg_x / wg_dy */
     int64_t woff[CNN_LAYERS], boff[CNN_LAYERS], nparams = 0;
     int adam_t = 0;
     int sms = 1;
@@ -514,6 +656,45 @@ pct_status make_act_map(CUtensorMap* m, void* ptr, int C, int height, int depth)
                           CU_TENSOR_MAP_INTERLEAVE_NONE, C == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return pct_fail(PCT_ERR_CUDA, "cuTensorMapEncodeTiled (activations, C=%d): %d", C, (int)r);
+    return PCT_OK;
+}
+
+/* Channel-major [c][z][y][x] bf16 with `C` channel rows: box = 32 voxels of one x row x `box_c` channels */
+pct_status make_cm_map(CUtensorMap* m, void* ptr, int C, int box_c, int height, int depth) {
+    const cuuint64_t dims[4] = {(cuuint64_t)CNN_W, (cuuint64_t)height, (cuuint64_t)depth, (cuuint64_t)C};
+    const cuuint64_t strides[3] = {(cuuint64_t)CNN_W * 2, (cuuint64_t)CNN_W * 2 * height,
+                                   (cuuint64_t)CNN_W * 2 * height * depth};
+    const cuuint32_t box[4] = {(cuuint32_t)WG_CHUNK, 1, 1, (cuuint32_t)box_c};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, ptr, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return pct_fail(PCT_ERR_CUDA, "cuTensorMapEncodeTiled (channel-major, C=%d): %d", C, (int)r);
+    return PCT_OK;
+}
+
+template <int CIN, int COUT>
+pct_status launch_wgrad(pct_cnn* n, const uint16_t* x, const uint16_t* dy, const CUtensorMap& xs_map,
+                        const CUtensorMap& dt_map) {
+    constexpr int smem = WgSmem<CIN, COUT>::TOTAL;
+    static bool attr = false;
+    if (!attr) {
+        PCT_CUDA(cudaFuncSetAttribute(k_conv_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    n->launches += 3;
+    k_wg_shift<CIN><<<pct_grid_for(n->nv, 256), 256, 0, n->stream>>>(n->nv, x, n->wg_x.as<uint16_t>());
+    k_wg_dyt<COUT><<<pct_grid_for(n->nv, 256), 256, 0, n->stream>>>(n->nv, dy, n->wg_dy.as<uint16_t>());
+    WgArgs a;
+    a.height = n->height;
+    a.chunks = n->depth * n->height * (CNN_W / WG_CHUNK);
+    const int want = a.chunks < n->sms ? a.chunks : n->sms;
+    a.per = (a.chunks + want - 1) / want;
+    const int grid = (a.chunks + a.per - 1) / a.per;
+    a.dw = n->gpad.as<float>();
+    a.err = n->err.as<unsigned long long>();
+    k_conv_wgrad<CIN, COUT><<<grid, CONV_THREADS, smem, n->stream>>>(xs_map, dt_map, a);
+    PCT_CUDA(cudaGetLastError());
     return PCT_OK;
 }
 
@@ -587,23 +768,18 @@ pct_status backward(pct_cnn* n) {
     ++n->launches;
     k_cnn_loss<<<2 * n->sms, 256, 0, n->stream>>>(n->nv, n->out.as<float>(), n->target.as<float>(),
                                                   n->dy8.as<uint16_t>(), n->loss.as<double>());
-    const int rows = n->depth * n->height;
-    const int slabs = (rows + 31) / 32;
     for (int l = CNN_LAYERS - 1; l >= 0; --l) {
         const uint16_t* dy = l == CNN_LAYERS - 1 ? n->dy8.as<uint16_t>() : n->dyl[l].as<uint16_t>();
         const int cin_p = LCIN[l], cout_p = LCOUT[l];
         PCT_CUDA(cudaMemsetAsync(n->gpad.p, 0, sizeof(float) * CNN_TAPS * cin_p * cout_p, n->stream));
         PCT_CUDA(cudaMemsetAsync(n->bgrad.p, 0, sizeof(float) * 32, n->stream));
-        n->launches += 3;
         if (l == 0)
-            k_conv_wgrad<16, 32><<<CNN_TAPS * slabs, 256, 0, n->stream>>>(n->depth, n->height, 32, layer_input(n, l),
-                                                                         dy, n->gpad.as<float>());
+            PCT_TRY((launch_wgrad<16, 32>(n, layer_input(n, l), dy, n->map_xs16, n->map_dt32)));
         else if (l == CNN_LAYERS - 1)
-            k_conv_wgrad<32, 16><<<CNN_TAPS * slabs, 256, 0, n->stream>>>(n->depth, n->height, 32, layer_input(n, l),
-                                                                         dy, n->gpad.as<float>());
+            PCT_TRY((launch_wgrad<32, 16>(n, layer_input(n, l), dy, n->map_xs32, n->map_dt16)));
         else
-            k_conv_wgrad<32, 32><<<CNN_TAPS * slabs, 256, 0, n->stream>>>(n->depth, n->height, 32, layer_input(n, l),
-                                                                         dy, n->gpad.as<float>());
+            PCT_TRY((launch_wgrad<32, 32>(n, layer_input(n, l), dy, n->map_xs32, n->map_dt32)));
+        n->launches += 2;
         if (cout_p == 16)
             k_conv_bgrad<16><<<n->sms, 256, 0, n->stream>>>(n->nv, dy, n->bgrad.as<float>());
         else
@@ -682,7 +858,8 @@ extern "C" pct_status pct_cnn_destroy(pct_cnn* n) {
     cudaSetDevice(n->device);
     if (n->stream) cudaStreamSynchronize(n->stream);
     DevBuf* bufs[] = {&n->in0, &n->out, &n->dy8, &n->x0, &n->hull, &n->target, &n->params,
-                      &n->grads, &n->adam_m, &n->adam_v, &n->gpad, &n->bgrad, &n->loss, &n->err, &n->scratch};
+                      &n->grads, &n->adam_m, &n->adam_v, &n->gpad, &n->bgrad, &n->loss, &n->err, &n->scratch,
+                      &n->wg_x, &n->wg_dy};
     for (DevBuf* b : bufs) b->release();
     for (int l = 0; l < CNN_LAYERS; ++l) {
         n->wf[l].release();
@@ -746,6 +923,8 @@ extern "C" pct_status pct_cnn_create(int device, int depth, int height, int widt
     if (st == PCT_OK) st = n->loss.alloc(8);
     if (st == PCT_OK) st = n->err.alloc(8);
     if (st == PCT_OK) st = n->scratch.alloc(nv * 32 * 4);
+    if (st == PCT_OK) st = n->wg_x.alloc(nv * 3 * 32 * 2);
+    if (st == PCT_OK) st = n->wg_dy.alloc(nv * 32 * 2);
     for (int l = 0; l < CNN_LAYERS && st == PCT_OK; ++l) {
         st = n->wf[l].alloc((size_t)CNN_TAPS * LCIN[l] * LCOUT[l] * 2);
         if (st == PCT_OK && l > 0) st = n->wt[l].alloc((size_t)CNN_TAPS * LCIN[l] * LCOUT[l] * 2);
@@ -767,6 +946,10 @@ extern "C" pct_status pct_cnn_create(int device, int depth, int height, int widt
         st = make_w_map(&n->map_wf[l], n->wf[l].p, LCIN[l], LCOUT[l]);
         if (st == PCT_OK && l > 0) st = make_w_map(&n->map_wt[l], n->wt[l].p, LCOUT[l], LCIN[l]);
     }
+    if (st == PCT_OK) st = make_cm_map(&n->map_xs16, n->wg_x.p, 3 * 16, 16, height, depth);
+    if (st == PCT_OK) st = make_cm_map(&n->map_xs32, n->wg_x.p, 3 * 32, 32, height, depth);
+    if (st == PCT_OK) st = make_cm_map(&n->map_dt16, n->wg_dy.p, 16, 16, height, depth);
+    if (st == PCT_OK) st = make_cm_map(&n->map_dt32, n->wg_dy.p, 32, 32, height, depth);
     if (st == PCT_OK) st = publish(n);
     if (st == PCT_OK && cudaStreamSynchronize(n->stream) != cudaSuccess) st = pct_fail(PCT_ERR_CUDA, "pct_cnn_create");
     if (st != PCT_OK) return fail(st);
