@@ -35,7 +35,8 @@
  *       on an aligned x); per 32-voxel chunk the 27 taps' boxes and dY's box
  *       fill a stage, 128 / CIN taps make one M = 128 tile, and the 7 (or 4)
  *       tiles accumulate in TMEM over the CTA's chunks; the epilogue adds the
- *       CTA's partial sums to dW with fp32 atomics.
+ *       CTA's partial sums to dW with fp32 atomics.  A row of ones in the
+ *       last tile's spare rows gives the bias gradient sum_v dY[v][co].
  *   k_adam, k_publish      Adam on the fp32 master weights, then the bf16
  *       copies in both tap orders.
  */
@@ -437,6 +438,7 @@ struct WgSmem {
 struct WgArgs {
     int height, chunks, per; /* 4 chunks per x row; this CTA: chunks [blockIdx.x * per, + per) */
     float* dw;               /* [tap][COUT][CIN] fp32, accumulated */
+    float* db;               /* [COUT] fp32, accumulated: the bias gradient */
     unsigned long long* err;
 };
 
@@ -453,11 +455,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv_wgrad(const __grid_con
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c0 = blockIdx.x * p.per;
     const int c1 = c0 + p.per < p.chunks ? c0 + p.per : p.chunks;
-    /* the missing taps of the last tile read zeros */
+    /* the missing taps of the last tile read zeros, except the first row of the first
+     * missing tap, which reads ones: its D row is sum_v dY[v][co], the bias gradient
+     * (a row of equal values is the same under the 64-byte swizzle) */
     constexpr int PAD = L::A_BYTES - CNN_TAPS * L::A_BOX;
+    constexpr uint32_t ONES = 0x3F803F80u; /* two bf16 1.0 */
     for (int st = 0; st < WG_STAGES; ++st)
         for (int k = threadIdx.x; k < PAD / 16; k += CONV_THREADS)
-            reinterpret_cast<uint4*>(smem + st * L::STAGE + CNN_TAPS * L::A_BOX)[k] = make_uint4(0u, 0u, 0u, 0u);
+            reinterpret_cast<uint4*>(smem + st * L::STAGE + CNN_TAPS * L::A_BOX)[k] =
+                k < 4 ? make_uint4(ONES, ONES, ONES, ONES) : make_uint4(0u, 0u, 0u, 0u);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (threadIdx.x == 0) {
         for (int st = 0; st < WG_STAGES; ++st) {
@@ -532,10 +538,14 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv_wgrad(const __grid_con
                 if (COUT > 16) tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(m * COUT) + 16, v + 16);
                 tmem_wait_ld();
                 const int tap = m * L::TPT + tl;
-                if (tap < CNN_TAPS)
+                if (tap < CNN_TAPS) {
 #pragma unroll
                     for (int co = 0; co < COUT; ++co)
                         atomicAdd(p.dw + ((size_t)tap * COUT + co) * CIN + ci, __uint_as_float(v[co]));
+                } else if (tap == CNN_TAPS && ci == 0) { /* the row of ones: the bias gradient */
+#pragma unroll
+                    for (int co = 0; co < COUT; ++co) atomicAdd(p.db + co, __uint_as_float(v[co]));
+                }
             }
             tc_fence_before();
         }
@@ -546,23 +556,6 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv_wgrad(const __grid_con
     if (warp == 0) {
         tc_fence_after();
         tmem_dealloc(tmem, L::TCOLS);
-    }
-}
-
-/* db[c] += sum_v dY[v][c] */
-template <int COUT>
-__global__ void k_conv_bgrad(int64_t nv, const uint16_t* __restrict__ dy, float* __restrict__ db) {
-    float s[COUT];
-#pragma unroll
-    for (int c = 0; c < COUT; ++c) s[c] = 0.0f;
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x)
-#pragma unroll
-        for (int c = 0; c < COUT; ++c) s[c] += bf(dy[v * COUT + c]);
-#pragma unroll
-    for (int c = 0; c < COUT; ++c) {
-        float t = s[c];
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(db + c, t);
     }
 }
 
@@ -692,6 +685,7 @@ pct_status launch_wgrad(pct_cnn* n, const uint16_t* x, const uint16_t* dy, const
     a.per = (a.chunks + want - 1) / want;
     const int grid = (a.chunks + a.per - 1) / a.per;
     a.dw = n->gpad.as<float>();
+    a.db = n->bgrad.as<float>();
     a.err = n->err.as<unsigned long long>();
     k_conv_wgrad<CIN, COUT><<<grid, CONV_THREADS, smem, n->stream>>>(xs_map, dt_map, a);
     PCT_CUDA(cudaGetLastError());
@@ -779,11 +773,7 @@ pct_status backward(pct_cnn* n) {
             PCT_TRY((launch_wgrad<32, 16>(n, layer_input(n, l), dy, n->map_xs32, n->map_dt16)));
         else
             PCT_TRY((launch_wgrad<32, 32>(n, layer_input(n, l), dy, n->map_xs32, n->map_dt32)));
-        n->launches += 2;
-        if (cout_p == 16)
-            k_conv_bgrad<16><<<n->sms, 256, 0, n->stream>>>(n->nv, dy, n->bgrad.as<float>());
-        else
-            k_conv_bgrad<32><<<n->sms, 256, 0, n->stream>>>(n->nv, dy, n->bgrad.as<float>());
+        ++n->launches;
         const int nw = CNN_TAPS * RCIN[l] * RCOUT[l];
         k_unpad_grad<<<pct_grid_for(nw, 256), 256, 0, n->stream>>>(RCIN[l], RCOUT[l], cin_p, cout_p,
                                                                    n->gpad.as<float>(),

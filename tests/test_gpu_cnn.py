@@ -176,3 +176,40 @@ def test_adam_steps_reduce_the_loss():
     losses = [net.train_step(x0, hull, target, 2e-3) for _ in range(150)]
     net.close()
     assert losses[-1] < 0.1 * losses[0], losses[::25]
+
+
+def test_weight_gradients_with_many_chunks_per_cta():
+    """At 8 x 64 x 128 voxels each CTA of the weight-gradient kernel accumulates 14
+    voxel chunks through its 3-stage ring (the small volume above gives 2): the
+    weight and bias gradients of a hidden layer against binary64."""
+    d, h = 8, 64
+    rng = np.random.default_rng(9)
+    net = cnn.Net(d, h, W)
+    net.init(4)
+    p = net.params()
+    sl = cnn.param_slices()
+    for k, (ws, shape, bs) in enumerate(sl):
+        p[bs] = rng.uniform(-0.1, 0.1, shape[1]).astype(np.float32)
+        if k == len(cnn.LAYERS) - 1:
+            p[ws] = rng.uniform(-0.05, 0.05, int(np.prod(shape))).astype(np.float32)
+    net.set_params(p)
+    zz, yy, xx = np.meshgrid(np.arange(d), np.arange(h), np.arange(W), indexing="ij")
+    hull = (((xx - 64) ** 2 + (yy - 32) ** 2) < 50 ** 2).astype(np.uint8)
+    x0 = (rng.uniform(0.5, 1.5, (d, h, W)) * hull).astype(np.float32)
+    target = (x0 + 0.2 * hull * np.cos(yy / 7.0)).astype(np.float32)
+    loss, g = net.gradients(x0, hull, target)
+    for l in (3, 7):
+        ws, shape, bs = sl[l]
+        cout, cin = shape[1], shape[2]
+        x = net.inspect(0, l - 1)[..., :cin].astype(np.float64).reshape(d, h, W, cin)
+        dy = net.inspect(1, l)[..., :cout].astype(np.float64).reshape(d, h, W, -1)[..., :cout]
+        xp = np.pad(x, ((1, 1), (1, 1), (1, 1), (0, 0)))
+        dw = np.empty((TAPS, cout, cin))
+        for t in range(TAPS):
+            dz, dyy, dx = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
+            xs = xp[1 + dz:1 + dz + d, 1 + dyy:1 + dyy + h, 1 + dx:1 + dx + W]
+            dw[t] = np.einsum("zyxo,zyxi->oi", dy, xs)
+        err = rel_l2(g[ws].reshape(shape), dw)
+        assert err <= 1e-5, "dW of layer %d: %.3g" % (l, err)
+        assert rel_l2(g[bs], dy.sum(axis=(0, 1, 2))) <= 1e-5, "db of layer %d" % l
+    net.close()
