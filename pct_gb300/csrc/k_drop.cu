@@ -511,8 +511,10 @@ pct_status pct_drop_prepare(pct_ctx* c) {
     if (!c->diag_ready) {
         pct_drop_release_graph(c);
         c->td.release();
-        pct_drop_gather_release(c);
         const int form = c->cfg.drop_form;
+        /* the gather form's buffers are kept for its next build (they only grow) */
+        if (form != PCT_DROP_GATHER) pct_drop_gather_release(c);
+        c->gather_entries = 0;
         if (form == PCT_DROP_TILED && !c->allreduce && c->num_shards == 1 && pct_drop_tiled_fits(c)) {
             PCT_TRY(pct_drop_tiled_build(c));
             const int64_t B = c->cfg.block_size;

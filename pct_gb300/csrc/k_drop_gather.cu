@@ -130,20 +130,44 @@ __global__ void k_jds_steps(int nv, int S, int kcap, const uint32_t* __restrict_
 }
 
 /* The transposed incidence of one block: every row entry's rank at its
- * voxel's next free step (one warp per row). */
+ * voxel's next free step.  A warp takes FILL_ROWS consecutive ranks (rows of
+ * neighbouring sinogram bins, most of them in one bin, whose paths cross
+ * nearly the same voxels) and walks them in windows of FILL_WIN entries per
+ * row; lanes that hold the same voxel claim their steps with one atomic
+ * (match_any), so that a voxel the rows share costs one L2 atomic, not one per
+ * row.  (A row that revisits a voxel inside a window claims two steps, as the
+ * reference adds twice.) */
+constexpr int FILL_ROWS = 4;
+constexpr int FILL_WIN = 32 / FILL_ROWS;
 __global__ void k_gather_fill(int nrows, const int64_t* __restrict__ mstart, const int* __restrict__ mlen,
                               const uint32_t* __restrict__ rows, uint32_t nv, const int64_t* __restrict__ slice_off,
                               int kcap, const uint32_t* __restrict__ ptab, const uint8_t* __restrict__ pos,
                               uint32_t* __restrict__ cursor, uint32_t* __restrict__ lists) {
-    const int j = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int g = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (j >= nrows) return;
-    const int64_t a = mstart[j];
-    const int len = mlen[j];
-    for (int q = lane; q < len; q += 32) {
-        const uint32_t v = rows[a + q];
-        if (v < nv) {
-            const uint32_t k = atomicAdd(cursor + v, 1u);
+    const int j0 = g * FILL_ROWS;
+    if (j0 >= nrows) return; /* the whole warp */
+    const int j = j0 + lane / FILL_WIN, o = lane % FILL_WIN;
+    int64_t a = 0;
+    int len = 0;
+    if (j < nrows) {
+        a = mstart[j];
+        len = mlen[j];
+    }
+    int maxlen = len;
+    for (int d = 16; d > 0; d >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, d));
+    for (int e0 = 0; e0 < maxlen; e0 += FILL_WIN) {
+        const int q = e0 + o;
+        const uint32_t v = q < len ? rows[a + q] : 0xffffffffu;
+        const bool act = v < nv;
+        const uint32_t key = act ? v : nv + (uint32_t)lane; /* inactive lanes stay alone */
+        const unsigned grp = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if (act && lane == leader) base = atomicAdd(cursor + v, (uint32_t)__popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (act) {
+            const uint32_t k = base + (uint32_t)__popc(grp & ((1u << lane) - 1u));
             const uint32_t s = v >> 5;
             lists[slice_off[s] + ptab[(size_t)s * kcap + k] + pos[v]] = (uint32_t)j;
         }
@@ -370,14 +394,12 @@ pct_status pct_drop_gather_build(pct_ctx* c) {
         c->launches += 2;
         k_jds_steps<<<pct_grid_for((int64_t)S * 32, 256), 256, 0, c->stream>>>(
             nv, S, kcap, c->gather_slot.as<uint32_t>() + (size_t)k * S * 32, pos, ptab);
-        k_gather_fill<<<pct_grid_for((e - s) * 32, 256), 256, 0, c->stream>>>(
+        k_gather_fill<<<pct_grid_for((e - s + FILL_ROWS - 1) / FILL_ROWS * 32, 256), 256, 0, c->stream>>>(
             (int)(e - s), m.start + s, m.len + s, c->rows.as<uint32_t>(), (uint32_t)nv,
             c->gather_off.as<int64_t>() + (size_t)k * S, kcap, ptab, pos, cursor, c->gather_lists.as<uint32_t>());
     }
     PCT_CUDA(cudaGetLastError());
     PCT_CUDA(cudaStreamSynchronize(c->stream));
-    c->gather_tmp.release();
-    c->gather_steps.release();
     return PCT_OK;
 }
 
