@@ -1,6 +1,7 @@
 """Edge cases of the reconstruction path (needs a GPU): empty and one-history
 scans, scans that miss the volume, zero-size and ragged chunks, a block size of
-one row and one larger than the scan, grids whose size is not a multiple of
+one row and one larger than the scan, the gather form on one block with
+hundreds of rows per voxel, grids whose size is not a multiple of
 the brick (no bricks; NUM_VOXELS not a multiple of 4), the linear voxel order,
 early stopping on the residual, and the status codes of out-of-order stages
 and invalid settings."""
@@ -92,6 +93,27 @@ def test_block_size_extremes_against_oracle(block):
     r.drop(1)
     x = r.array("X").astype(np.float64)
     r.close()
+    ref = ora["x_1"]
+    assert np.linalg.norm(x - ref) <= DROP_TOL * np.linalg.norm(ref)
+
+
+def test_gather_form_with_long_columns_against_oracle():
+    """One block of every row on a small grid: hundreds of rows per voxel, so
+    the gather form's column lists run to thousands of words per slice of 32
+    voxels and hundreds of jagged-diagonal steps; the image still matches the
+    oracle."""
+    w = phantoms.tiny(num_histories=300000, seed=12, v_extent=0.3)
+    cfg = _cfg(w, iterations=1, block_size=10_000_000, drop_form=3)
+    data, angles = phantoms.generate(w)
+    ora = oracle.run_pipeline(cfg, data, angles, iterations=1)
+    r = _through_rows(cfg, data, angles)
+    st = r.drop(1)
+    counts = r.counts()
+    x = r.array("X").astype(np.float64)
+    r.close()
+    assert st.drop_form == 3
+    slices = (x.size + 31) // 32
+    assert counts["drop_list_entries"] / slices > 8 * 1024  # long slices on average
     ref = ora["x_1"]
     assert np.linalg.norm(x - ref) <= DROP_TOL * np.linalg.norm(ref)
 
