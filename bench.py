@@ -48,9 +48,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--histories", type=int, default=None,
                     help="scan size (default: 30M for cfg2, 60M for cfg4)")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg4", "cfg5"],
-                    help="cfg2 (the bench line: 256x256x32, 8-insert cylinder), cfg4 (320x320x64 head phantom) or "
-                         "cfg5 (learned warm start: train the CNN, compare FBP-start and learned-start DROP)")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"],
+                    help="cfg2 (the bench line: 256x256x32, 8-insert cylinder), cfg3 (16 batched ellipsoid scans, "
+                         "2M-40M histories, DROP of all of them in one persistent launch per iteration), cfg4 "
+                         "(320x320x64 head phantom) or cfg5 (learned warm start: train the CNN, compare FBP-start "
+                         "and learned-start DROP)")
+    ap.add_argument("--scans", type=int, default=16, help="cfg3: number of scans")
     ap.add_argument("--train-phantoms", type=int, default=64, help="cfg5: training phantoms")
     ap.add_argument("--eval-phantoms", type=int, default=8, help="cfg5: held-out phantoms")
     ap.add_argument("--train-steps", type=int, default=3000, help="cfg5: Adam steps")
@@ -330,9 +333,87 @@ def run_warmstart(a, ws, rank):
     print(json.dumps(out))
 
 
+def run_batched(a, ws, rank):
+    """--workload cfg3: many uneven scans on one GPU.  `--scans` seeded ellipsoid scans (histories
+    log-uniform in 2M-40M, grids drawn per seed) are prepared through their MLP rows (rows packed),
+    each gets its DROP block size from autotune_block_size, and a step is the DROP phase of all of
+    them: 12 iterations of every scan from its initial iterate in one persistent cooperative launch
+    per iteration, one captured graph per iteration (pct_drop_many).  The step time is the
+    library's CUDA-event time on the launching stream; `value` = recon histories of all scans x 12
+    / step time.  The same phase with one context after another and with concurrent contexts (a
+    host thread and stream each; wall clock) is given beside it."""
+    if rank != 0:
+        return
+    import math
+    import random
+
+    import torch
+    from pct_gb300 import batch, phantoms, recon
+    torch.cuda.set_device(0)
+    rng = random.Random(100)
+    rs, meta = [], []
+    try:
+        for k in range(a.scans):
+            n = int(round(math.exp(rng.uniform(math.log(2e6), math.log(40e6)))))
+            w = phantoms.ellipsoids(100 + k, num_histories=n)
+            data, angles = phantoms.generate(w)
+            cfg = phantoms.make_config(w.config)
+            rs += batch.prepare_scans([(cfg, data, angles)])
+            del data, angles
+            g = phantoms.geometry(cfg)
+            best, _ = batch.autotune_block_size(rs[-1])
+            meta.append({"seed": 100 + k, "histories": n, "grid": "%dx%dx%d" % (g.columns, g.rows, g.slices),
+                         "recon_histories": rs[-1].counts()["reconstruction_histories"], "block_size": best})
+        iters = int(rs[0].cfg.iterations)
+        units = sum(m["recon_histories"] for m in meta) * iters
+
+        def step():
+            for r in rs:
+                r.reset_iterate()
+            st = recon.drop_many(rs, iters)
+            return st[0].seconds
+
+        for _ in range(a.warmup):
+            step()
+        with Clocks(0) as clk:
+            times = [step() for _ in range(a.steps)]
+        launches = a.steps * iters * 2  # per iteration: k_drop_many and k_many_store_resid
+        sec = float(np.mean(times))
+        other = {}
+        for mode in ("sequential", "concurrent"):
+            t, _ = batch.drop_phase(rs, iters, mode)
+            other[mode] = {"seconds_wall": t, "histories_iterations_per_second": units / t}
+    finally:
+        for r in rs:
+            r.close()
+    out = {"metric": "histories/s per DROP iteration (all scans)", "value": units / sec, "unit": UNIT,
+           "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded ellipsoid phantoms)",
+           "config": {"workload": "cfg3: %d ellipsoid scans (seeds 100-%d), %d-%d histories log-uniform in 2M-40M, "
+                                  "%d recon histories in all, grids %s, %d DROP iterations, block size per scan by "
+                                  "autotune_block_size" % (a.scans, 99 + a.scans, min(m["histories"] for m in meta),
+                                                           max(m["histories"] for m in meta), units // iters,
+                                                           sorted({m["grid"] for m in meta}), iters),
+                      "l2": "inputs larger than L2 (rows of all scans resident)",
+                      "step": "pct_drop_many: one cooperative launch per iteration over every scan's blocks, one "
+                              "captured graph per iteration; CUDA events on the launching stream",
+                      "scans": meta},
+           "other_modes": other, "gpu_launches": int(launches), "clocks": clk.summary()}
+    print(json.dumps(out))
+
+
 def main():
     a = parse()
     ws, rank, local = dist_env()
+    if a.workload == "cfg3":
+        if a.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference runs one scan per block loop; "
+                                                                      "no batched form to time"}))
+            return
+        run_batched(a, ws, rank)
+        return
     if a.workload == "cfg5":
         if a.impl == "reference":
             if rank == 0:
