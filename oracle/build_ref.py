@@ -62,6 +62,16 @@ GEOMETRIES = {
         "GANTRY_ANGLE_INTERVAL": "2.0",
         "ANGULAR_BIN_SIZE": "2.0",
     },
+    # Config 4's head-phantom grid: 320x320x64 at 0.8x0.8x2.5 mm, r = 12.8 cm,
+    # 2 degree steps (180 angles).
+    "cfg4": {
+        "RECON_CYL_RADIUS": "12.8",
+        "COLUMNS": "320",
+        "ROWS": "320",
+        "SSD_V_SIZE": "17.0",
+        "GANTRY_ANGLE_INTERVAL": "2.0",
+        "ANGULAR_BIN_SIZE": "2.0",
+    },
     # Smallest grid of the batched-scan family: 128x128x8 at 1x1x2.5 mm,
     # r = 6.4 cm, 2 degree steps (180 angles).
     "cfg3_128x8": {

@@ -63,6 +63,9 @@ def scenarios():
         # the benchmark scan's geometry and phantom (256x256x32, 180 angles), through the MLP rows
         "cfg2_grid": dict(geometry="cfg2", workload=phantoms.cfg2(num_histories=200000, seed=9),
                           run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=0), mlp_rows=1500),
+        # config 4's head phantom and grid (320x320x64, 0.8 mm voxels, 180 angles), through the MLP rows
+        "cfg4_grid": dict(geometry="cfg4", workload=phantoms.cfg4(num_histories=200000, seed=9),
+                          run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=0), mlp_rows=1500),
         # ellipsoid phantom of the batched-scan family on its smallest grid, 180 angles, through DROP
         "cfg3_128x8": dict(geometry="cfg3_128x8",
                            workload=phantoms.ellipsoids(31, num_histories=150000, cols=128, slices=8),
@@ -81,15 +84,15 @@ def digest(a):
     return hashlib.sha256(a.tobytes()).hexdigest()
 
 
-def pack(name, arr, out, full_limit=FULL_LIMIT):
+def pack(name, arr, out, full_limit=FULL_LIMIT, pins=False):
     out["dtype:" + name] = np.array(str(arr.dtype))
     out["shape:" + name] = np.array(arr.shape, dtype=np.int64)
     out["sha:" + name] = np.array(digest(arr))
     # DROP iterates x_1, x_2, ... in full whatever their size: they are compared
-    # within a tolerance, not by digest; so are the pinned DROP loops, and x_0 and
-    # the endpoint file are inputs of the pin tests
+    # within a tolerance, not by digest; so are the pinned DROP loops, and (in a
+    # scenario with pins) x_0 and the endpoint file, inputs of the pin tests
     if (arr.size <= full_limit or (name.startswith("x_") and name[2:].isdigit() and int(name[2:]) > 0)
-            or name == "x_0" or (name.startswith("pin.") and name != "pin.tab.rows")):
+            or (pins and name == "x_0") or (name.startswith("pin.") and name != "pin.tab.rows")):
         out["full:" + name] = arr
     else:
         out["head:" + name] = arr.ravel()[:SAMPLE]
@@ -193,7 +196,7 @@ def make(name, sc, ref_root):
     for k, v in res.items():
         if k.startswith("__"):
             continue
-        pack(k, v, out, sc.get("full_limit", FULL_LIMIT))
+        pack(k, v, out, sc.get("full_limit", FULL_LIMIT), pins=bool(sc.get("pins")))
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     print("%s: %d arrays, %d bytes" % (path, len(res), os.path.getsize(path)))

@@ -33,7 +33,7 @@ BINS = [("bin_counts_h_pre", "BIN_COUNTS_PRE"), ("mean_WEPL_h", "MEAN_WEPL"), ("
         ("mean_rel_uv_angle_h", "MEAN_UV"), ("stddev_WEPL_h", "SD_WEPL"), ("stddev_rel_ut_angle_h", "SD_UT"),
         ("stddev_rel_uv_angle_h", "SD_UV"), ("bin_counts_post", "BIN_COUNTS_POST"),
         ("bin_counts_pre", "BIN_COUNTS_POST"), ("sinogram", "SINOGRAM")]
-WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1, "cfg2": phantoms.cfg2}
+WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1, "cfg2": phantoms.cfg2, "cfg4": phantoms.cfg4}
 
 
 def sha(a):
@@ -58,6 +58,7 @@ def golden(request):
     data, angles = phantoms.generate(w)
     assert sha(data) + sha(angles) == str(fx["input_sha"]), "synthetic inputs differ from the fixture's"
     cfg = phantoms.make_config(w.config)
+    cfg.chord_bf16 = 0  # the reference's chords are binary32
     run = ast.literal_eval(str(fx["run_config"]))
     for k in ("msc_on", "sm_on", "sc_on", "mlp_hull"):
         if k in run:

@@ -26,6 +26,10 @@ CASES = {
     "cfg1_sm": lambda: (phantoms.cfg1(num_histories=120000, seed=5), dict(iterations=2)),
     # the benchmark's grid and phantom: 256x256x32 voxels, 180 angles
     "cfg2_grid": lambda: (phantoms.cfg2(num_histories=200000, seed=9), dict(iterations=2, block_size=50000)),
+    # config 4's head phantom and grid: 320x320x64 voxels of 0.8 mm, 180 angles (binary32
+    # chords here: the oracle's; the bfloat16 chords are checked by test_bf16_chords_error_stated)
+    "cfg4_grid": lambda: (phantoms.cfg4(num_histories=200000, seed=9),
+                          dict(iterations=2, block_size=50000, chord_bf16=0)),
     # config 3 grids at both ends: ellipsoid phantoms on 128x128x8 and 256x256x48
     "cfg3_128x8": lambda: (phantoms.ellipsoids(31, num_histories=150000, cols=128, slices=8),
                            dict(iterations=2, block_size=50000)),

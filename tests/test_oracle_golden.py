@@ -20,7 +20,7 @@ from oracle import oracle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
-WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1, "cfg2": phantoms.cfg2}
+WORKLOADS = {"tiny": phantoms.tiny, "cfg1": phantoms.cfg1, "cfg2": phantoms.cfg2, "cfg4": phantoms.cfg4}
 DROP_TOL = 1e-6
 
 
@@ -56,6 +56,7 @@ def oracle_outputs(fx):
     data, angles = phantoms.generate(w)
     assert sha(data) + sha(angles) == str(fx["input_sha"]), "synthetic inputs differ from the fixture's"
     cfg = phantoms.make_config(w.config)
+    cfg.chord_bf16 = 0  # the reference's chords are binary32
     run = run_kwargs(fx)
     for k in ("msc_on", "sm_on", "sc_on", "mlp_hull"):
         if k in run:
