@@ -72,6 +72,16 @@ GEOMETRIES = {
         "GANTRY_ANGLE_INTERVAL": "2.0",
         "ANGULAR_BIN_SIZE": "2.0",
     },
+    # Largest grid of the batched-scan family: 256x256x48 at 1x1x2.5 mm,
+    # r = 12.8 cm, 2 degree steps (180 angles).
+    "cfg3_256x48": {
+        "RECON_CYL_RADIUS": "12.8",
+        "COLUMNS": "256",
+        "ROWS": "256",
+        "SSD_V_SIZE": "13.0",
+        "GANTRY_ANGLE_INTERVAL": "2.0",
+        "ANGULAR_BIN_SIZE": "2.0",
+    },
     # Smallest grid of the batched-scan family: 128x128x8 at 1x1x2.5 mm,
     # r = 6.4 cm, 2 degree steps (180 angles).
     "cfg3_128x8": {
@@ -151,7 +161,7 @@ def build(ref_root, geometry, verbose=False):
            "-I", os.path.join(HERE, "ref", "cuda_emul"),
            "-I", os.path.join(HERE, "ref"),
            "-I", os.path.join(ref_root, "include"),
-           "-x", "c++", "-", "-o", so, "-fopenmp"]
+           "-x", "c++", "-", "-o", so, "-fopenmp", "-lquadmath"]
     if verbose:
         print(" ".join(cmd))
     r = subprocess.run(cmd, input=src.encode("latin-1"), capture_output=True)

@@ -122,7 +122,8 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
 
         /* a2: recon_volume_intersections_GPU (.cu:2195-2299) */
         double rot = ga * PCT_ANGLE_TO_RADIANS;
-        double cr = pct_cos(rot), sr = pct_sin(rot);
+        double cr, sr;
+        pct_sincos_cr(rot, &sr, &cr); /* binary64 cos and sin, correctly rounded */
         double ut_entry_angle = pct_atan2f(t_in_2 - t_in_1, u_in_2 - u_in_1);
         double u_entry, t_entry, u_exit, t_exit;
         int entered = calculate_intercepts(&g, u_in_2, t_in_2, ut_entry_angle, &u_entry, &t_entry);
@@ -177,7 +178,9 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
         if (path_angle < 0) path_angle += 2 * PCT_PI;
         int angle_bin = pct_d2i((path_angle * PCT_RADIANS_TO_ANGLE / cfg->angular_bin_size) + 0.5) % g.angular_bins;
         double angle = angle_bin * cfg->angular_bin_size * PCT_ANGLE_TO_RADIANS;
-        double t = y_mid * pct_cos(angle) - x_mid * pct_sin(angle);
+        double s_a, c_a;
+        pct_sincos_cr(angle, &s_a, &c_a);
+        double t = y_mid * c_a - x_mid * s_a;
         int t_bin = pct_d2i((t / cfg->t_bin_size) + T2);
         double v = z_mid;
         int v_bin = pct_d2i((v / cfg->v_bin_size) + V2);
@@ -600,7 +603,8 @@ void ora_backprojection(const pct_config* cfg, const float* sino, float* image) 
         }
         float acc = 0.0f;
         for (int ab = 0; ab < g.angular_bins; ++ab) {
-            double ca = pct_cos(ab * delta), sa = pct_sin(ab * delta);
+            double ca, sa;
+            pct_sincos_cr(ab * delta, &sa, &ca);
             double u = x * ca + y * sa;
             double t = -x * sa + y * ca;
             double v = z;
@@ -962,8 +966,7 @@ static int ora_tables(void) {
     }
     for (int i = 0; i <= ORA_TRIG_N; ++i) {
         double val = ORA_TRIG_MIN + i * ORA_TRIG_STEP;
-        t[0][i] = pct_sin(val);
-        t[1][i] = pct_cos(val);
+        pct_sincos_cr(val, &t[0][i], &t[1][i]);
     }
     for (int k = 0; k <= ORA_DEPTH_N; ++k) {
         double du = k * ORA_DEPTH_STEP;

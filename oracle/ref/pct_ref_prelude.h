@@ -25,6 +25,11 @@
  *     (glibc 2.39 atan2f misrounds about one input in six; CUDA's atan2f is
  *     documented to 2 ulp), so the harness pins them to the exact value, the
  *     same definition the product and the oracle use;
+ *   - correctly rounded binary64 sin/cos (the binary128 libquadmath value
+ *     rounded once) for the same reason: glibc 2.39's sin and cos misround a
+ *     few of the per-angle arguments the reference tabulates (gantry rotation,
+ *     bin angles, backprojection), CUDA's are documented to 2 ulp, and the
+ *     product and the oracle build those tables correctly rounded;
  *   - the two shims the reference needs under a modern compiler:
  *     `syncthreads` (undefined in CUDA) and `std::ifstream == NULL`.
  */
@@ -32,6 +37,7 @@
 #define PCT_REF_PRELUDE_H
 
 #include <cmath>
+#include <quadmath.h>
 #include <cstdlib>
 #include <cstring>
 #include <cstdio>
@@ -98,6 +104,43 @@ using std::exp;
 using std::fabs;
 using std::floor;
 using std::ceil;
+/* sin and cos: binary64 correctly rounded; the float overloads as sinf/cosf.
+ * The reference takes sin and cos of the same angle at every MLP sample
+ * (.cu:5465) and of each projection angle for every voxel it backprojects
+ * (.cu:3180), so each thread remembers 4096 arguments of each (a
+ * direct-mapped table on a hash of the argument's bits): binary128 is slow. */
+enum { PCT_REF_MEMO = 4096 };
+struct pct_ref_memo {
+    unsigned long long key[PCT_REF_MEMO];
+    double val[PCT_REF_MEMO];
+    bool used[PCT_REF_MEMO];
+};
+inline double pct_ref_memo_get(pct_ref_memo& m, double x, __float128 (*f)(__float128)) {
+    unsigned long long k;
+    std::memcpy(&k, &x, sizeof k);
+    const unsigned long long h = k * 0x9E3779B97F4A7C15ull;
+    const int slot = (int)(h >> 52); /* 12 bits */
+    if (m.used[slot] && m.key[slot] == k) return m.val[slot];
+    const double v = (double)f((__float128)x);
+    m.key[slot] = k;
+    m.val[slot] = v;
+    m.used[slot] = true;
+    return v;
+}
+inline double pct_ref_sin(double x) {
+    static thread_local pct_ref_memo m = {};
+    return pct_ref_memo_get(m, x, sinq);
+}
+inline double pct_ref_cos(double x) {
+    static thread_local pct_ref_memo m = {};
+    return pct_ref_memo_get(m, x, cosq);
+}
+inline float pct_ref_sin(float x) { return pct_ref_sinf(x); }
+inline float pct_ref_cos(float x) { return pct_ref_cosf(x); }
+inline double pct_ref_sin(int x) { return pct_ref_sin((double)x); }
+inline double pct_ref_cos(int x) { return pct_ref_cos((double)x); }
+#define sin pct_ref_sin
+#define cos pct_ref_cos
 inline int max(int a, int b) { return a > b ? a : b; }
 inline int min(int a, int b) { return a < b ? a : b; }
 inline unsigned int max(unsigned int a, unsigned int b) { return a > b ? a : b; }

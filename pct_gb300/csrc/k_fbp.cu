@@ -151,7 +151,11 @@ __global__ void __launch_bounds__(128) k_backproject(DevGeom g, const float* __r
 
 __global__ void k_trig_bp(int n, double delta, double2* __restrict__ out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_double2(pct_cos(i * delta), pct_sin(i * delta));
+    if (i < n) {
+        double s, c;
+        pct_sincos_cr(i * delta, &s, &c); /* the reference's binary64 cos and sin, correctly rounded */
+        out[i] = make_double2(c, s);
+    }
 }
 
 __global__ void k_fbp_hull(DevGeom g, double thr, const float* __restrict__ image, uint8_t* __restrict__ hull) {

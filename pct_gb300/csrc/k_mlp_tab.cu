@@ -41,8 +41,7 @@ __global__ void k_tab_trig(int n, double* __restrict__ sin_t, double* __restrict
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i > n) return;
     const double val = TAB_TRIG_MIN + i * TAB_TRIG_STEP;
-    sin_t[i] = pct_sin(val);
-    cos_t[i] = pct_cos(val);
+    pct_sincos_cr(val, sin_t + i, cos_t + i); /* sin(val), cos(val) of .cu:4806-4807, correctly rounded */
 }
 
 /* depth[k * TP_COUNT + j]: the six depth tables interleaved per depth step */

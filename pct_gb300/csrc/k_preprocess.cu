@@ -64,7 +64,9 @@ __global__ void k_trig_table(double2* __restrict__ out, int n, double a, double 
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         double ang = (i * a) * b;
-        out[i] = make_double2(pct_cos(ang), pct_sin(ang));
+        double s, c;
+        pct_sincos_cr(ang, &s, &c); /* the reference's binary64 cos and sin, correctly rounded */
+        out[i] = make_double2(c, s);
     }
 }
 
@@ -85,7 +87,12 @@ __global__ void __launch_bounds__(256) k_preprocess(DevGeom g, In13 in, const fl
     int ga = ((int)proj[i] + 270) % 360;
     /* a2 (.cu:2198-2298) */
     double rot = ga * PCT_ANGLE_TO_RADIANS;
-    double2 cs = (ga >= 0 && ga < 360) ? trig_gantry[ga] : make_double2(pct_cos(rot), pct_sin(rot));
+    double2 cs;
+    if (ga >= 0 && ga < 360) {
+        cs = trig_gantry[ga];
+    } else {
+        pct_sincos_cr(rot, &cs.y, &cs.x);
+    }
     double cr = cs.x, sr = cs.y;
     double ut_entry = pct_atan2f(t_in_2 - t_in_1, u_in_2 - u_in_1);
     double u_e, t_e, u_x, t_x;
@@ -141,7 +148,7 @@ __global__ void __launch_bounds__(256) k_preprocess(DevGeom g, In13 in, const fl
         ab = trig_bins[angle_bin];
     } else {
         double angle = angle_bin * g.angular_bin_size * PCT_ANGLE_TO_RADIANS;
-        ab = make_double2(pct_cos(angle), pct_sin(angle));
+        pct_sincos_cr(angle, &ab.y, &ab.x);
     }
     double t = y_mid * ab.x - x_mid * ab.y;
     int t_bin = pct_d2i((t / g.t_bin_size) + (g.t_bins / 2));

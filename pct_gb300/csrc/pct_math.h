@@ -186,6 +186,85 @@ PCT_FN void pct_sincos(double x, double* s, double* c) {
         default: *s = -ck; *c = sk; break;
     }
 }
+/* ---- correctly rounded sin / cos for per-angle tables -------------------- */
+/* Double-double arithmetic: a value is hi + lo with |lo| <= ulp(hi) / 2. */
+PCT_FN void pct_dd_mul(double ah, double al, double bh, double bl, double* h, double* l) {
+    double p, e;
+    pct_two_prod(ah, bh, &p, &e);
+    e += ah * bl + al * bh;
+    pct_fast_two_sum(p, e, h, l);
+}
+PCT_FN void pct_dd_add(double ah, double al, double bh, double bl, double* h, double* l) {
+    double s, e;
+    pct_two_sum(ah, bh, &s, &e);
+    e += al + bl;
+    pct_fast_two_sum(s, e, h, l);
+}
+/* sin(x) and cos(x) rounded once from double-double values: the reduction of
+ * pct_rem_pio2 (x - k pi/2 = r + rr), then the Taylor series of sin and cos
+ * on |r| <= pi/4 to the terms r^25 / 25! and r^26 / 26! (the next ones are
+ * below 2^-100) in double-double Horner form with double-double 1/n!, and
+ * one final rounding of hi + lo.  About 100 correct bits before that
+ * rounding, so the result is the correctly rounded value unless sin or cos
+ * lies within 2^-100 (relative) of a rounding boundary.  For the per-angle
+ * tables where the reference takes the platform's binary64 cos and sin of an
+ * angle (gantry rotation, bin angles, backprojection); a few hundred calls
+ * per scan. */
+PCT_FN void pct_sincos_cr(double x, double* s, double* c) {
+    /* 1/n! as hi, lo: sine terms n = 1, 3, ..., 25, cosine terms n = 0, 2, ..., 26 */
+    const double SI[13][2] = {{1.0, 0.0},
+                              {0.16666666666666666, 9.25185853854297e-18},
+                              {0.008333333333333333, 1.1564823173178714e-19},
+                              {0.0001984126984126984, 1.7209558293420705e-22},
+                              {2.7557319223985893e-06, -1.858393274046472e-22},
+                              {2.505210838544172e-08, -1.448814070935912e-24},
+                              {1.6059043836821613e-10, 1.2585294588752098e-26},
+                              {7.647163731819816e-13, 7.03872877733453e-30},
+                              {2.8114572543455206e-15, 1.6508842730861433e-31},
+                              {8.22063524662433e-18, 2.2141894119604265e-34},
+                              {1.9572941063391263e-20, -1.3643503830087908e-36},
+                              {3.868170170630684e-23, -8.843177655482344e-40},
+                              {6.446950284384474e-26, -1.9330404233703465e-42}};
+    const double CO[14][2] = {{1.0, 0.0},
+                              {0.5, 0.0},
+                              {0.041666666666666664, 2.3129646346357427e-18},
+                              {0.001388888888888889, -5.300543954373577e-20},
+                              {2.48015873015873e-05, 2.1511947866775882e-23},
+                              {2.755731922398589e-07, 2.3767714622250297e-23},
+                              {2.08767569878681e-09, -1.20734505911326e-25},
+                              {1.1470745597729725e-11, 2.0655512752830745e-28},
+                              {4.779477332387385e-14, 4.399205485834081e-31},
+                              {1.5619206968586225e-16, 1.1910679660273754e-32},
+                              {4.110317623312165e-19, 1.4412973378659527e-36},
+                              {8.896791392450574e-22, -7.911402614872376e-38},
+                              {1.6117375710961184e-24, -3.6846573564509766e-41},
+                              {2.4795962632247976e-27, -1.2953730964765229e-43}};
+    double r, rr;
+    const int q = pct_rem_pio2(x, &r, &rr);
+    double zh, zl; /* z = -(r + rr)^2: the series alternate */
+    pct_dd_mul(r, rr, r, rr, &zh, &zl);
+    zh = -zh;
+    zl = -zl;
+    double sh = SI[12][0], sl = SI[12][1];
+    for (int k = 11; k >= 0; --k) {
+        pct_dd_mul(sh, sl, zh, zl, &sh, &sl);
+        pct_dd_add(sh, sl, SI[k][0], SI[k][1], &sh, &sl);
+    }
+    pct_dd_mul(sh, sl, r, rr, &sh, &sl); /* sin(r + rr) */
+    double ch = CO[13][0], cl = CO[13][1];
+    for (int k = 12; k >= 0; --k) {
+        pct_dd_mul(ch, cl, zh, zl, &ch, &cl);
+        pct_dd_add(ch, cl, CO[k][0], CO[k][1], &ch, &cl);
+    }
+    const double sk = sh + sl, ck = ch + cl;
+    switch (q) {
+        case 0: *s = sk; *c = ck; break;
+        case 1: *s = ck; *c = -sk; break;
+        case 2: *s = -sk; *c = -ck; break;
+        default: *s = -ck; *c = sk; break;
+    }
+}
+
 /* tan = sin/cos from double-double kernel values, one exact-remainder correction. */
 PCT_FN double pct_tan(double x) {
     double r, rr;

@@ -71,6 +71,10 @@ def scenarios():
                            workload=phantoms.ellipsoids(31, num_histories=150000, cols=128, slices=8),
                            run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=2, block_size=50000, lambda_=0.1),
                            mlp_rows=1500),
+        # the same family on its largest grid (256x256x48), through the MLP rows
+        "cfg3_256x48": dict(geometry="cfg3_256x48",
+                            workload=phantoms.ellipsoids(32, num_histories=300000, cols=256, slices=48),
+                            run=dict(msc_on=0, sm_on=1, mlp_hull=2, iterations=0), mlp_rows=1500),
         # a small in-slab scan whose reference-written endpoint file is stored in full,
         # with the tabulated MLP and the DROP variants of the CPU reconstruction
         "tiny_pins": dict(geometry="tiny", workload=phantoms.tiny(num_histories=16000, seed=13, v_extent=0.3),
