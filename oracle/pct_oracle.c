@@ -106,6 +106,20 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
     if (pct_geometry_derive(cfg, &g)) return 1;
     const double H = g.recon_cyl_height;
     const int T2 = g.t_bins / 2, V2 = g.v_bins / 2;
+    /* cos and sin of every whole gantry angle, correctly rounded, once (the
+     * same values for every history at that angle) */
+    static double trig_ga[360][2];
+    static int trig_ready = 0;
+#pragma omp critical(ora_trig_ga)
+    if (!trig_ready) {
+        for (int a = 0; a < 360; ++a) pct_sincos_cr(a * PCT_ANGLE_TO_RADIANS, &trig_ga[a][1], &trig_ga[a][0]);
+        trig_ready = 1;
+    }
+    /* and of every angle bin (this configuration's bin size) */
+    double* trig_bin = (double*)malloc(sizeof(double) * 2 * (size_t)(g.angular_bins > 0 ? g.angular_bins : 1));
+    if (!trig_bin) return 2;
+    for (int b = 0; b < g.angular_bins; ++b)
+        pct_sincos_cr(b * cfg->angular_bin_size * PCT_ANGLE_TO_RADIANS, &trig_bin[2 * b + 1], &trig_bin[2 * b]);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         /* a1: read_data_chunk_v02 unit conversion (.cu:1883-1897) and gantry angle (.cu:1921) */
@@ -122,8 +136,13 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
 
         /* a2: recon_volume_intersections_GPU (.cu:2195-2299) */
         double rot = ga * PCT_ANGLE_TO_RADIANS;
-        double cr, sr;
-        pct_sincos_cr(rot, &sr, &cr); /* binary64 cos and sin, correctly rounded */
+        double cr, sr; /* binary64 cos and sin, correctly rounded */
+        if (ga >= 0 && ga < 360) {
+            cr = trig_ga[ga][0];
+            sr = trig_ga[ga][1];
+        } else {
+            pct_sincos_cr(rot, &sr, &cr);
+        }
         double ut_entry_angle = pct_atan2f(t_in_2 - t_in_1, u_in_2 - u_in_1);
         double u_entry, t_entry, u_exit, t_exit;
         int entered = calculate_intercepts(&g, u_in_2, t_in_2, ut_entry_angle, &u_entry, &t_entry);
@@ -177,9 +196,13 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
         double path_angle = pct_atan2f(yx - ye, xx - xe);
         if (path_angle < 0) path_angle += 2 * PCT_PI;
         int angle_bin = pct_d2i((path_angle * PCT_RADIANS_TO_ANGLE / cfg->angular_bin_size) + 0.5) % g.angular_bins;
-        double angle = angle_bin * cfg->angular_bin_size * PCT_ANGLE_TO_RADIANS;
         double s_a, c_a;
-        pct_sincos_cr(angle, &s_a, &c_a);
+        if (angle_bin >= 0 && angle_bin < g.angular_bins) {
+            c_a = trig_bin[2 * angle_bin];
+            s_a = trig_bin[2 * angle_bin + 1];
+        } else {
+            pct_sincos_cr(angle_bin * cfg->angular_bin_size * PCT_ANGLE_TO_RADIANS, &s_a, &c_a);
+        }
         double t = y_mid * c_a - x_mid * s_a;
         int t_bin = pct_d2i((t / cfg->t_bin_size) + T2);
         double v = z_mid;
@@ -194,6 +217,7 @@ int ora_preprocess(const pct_config* cfg, int64_t n, const float* const in13[13]
             bin_valid[i] = 0;
         }
     }
+    free(trig_bin);
     return 0;
 }
 
@@ -590,6 +614,10 @@ void ora_backprojection(const pct_config* cfg, const float* sino, float* image) 
     const double delta = cfg->gantry_angle_interval * PCT_ANGLE_TO_RADIANS;
     const double SR = cfg->source_radius, R = g.recon_cyl_radius;
     const int ATB = g.angular_bins * g.t_bins;
+    /* cos and sin of every projection angle, correctly rounded, once */
+    double* trig = (double*)malloc(sizeof(double) * 2 * (size_t)(g.angular_bins > 0 ? g.angular_bins : 1));
+    if (!trig) return;
+    for (int ab = 0; ab < g.angular_bins; ++ab) pct_sincos_cr(ab * delta, &trig[2 * ab + 1], &trig[2 * ab]);
 #define SINO(k) (((k) >= 0 && (k) < g.num_bins) ? sino[(k)] : 0.0f)
 #pragma omp parallel for schedule(static)
     for (int voxel = 0; voxel < g.num_voxels; ++voxel) {
@@ -603,8 +631,7 @@ void ora_backprojection(const pct_config* cfg, const float* sino, float* image) 
         }
         float acc = 0.0f;
         for (int ab = 0; ab < g.angular_bins; ++ab) {
-            double ca, sa;
-            pct_sincos_cr(ab * delta, &sa, &ca);
+            const double ca = trig[2 * ab], sa = trig[2 * ab + 1];
             double u = x * ca + y * sa;
             double t = -x * sa + y * ca;
             double v = z;
@@ -628,6 +655,7 @@ void ora_backprojection(const pct_config* cfg, const float* sino, float* image) 
         image[voxel] = (float)(acc * delta);
     }
 #undef SINO
+    free(trig);
 }
 
 /* FBP_image_2_hull_GPU (.cu:3250-3261) */
