@@ -15,11 +15,16 @@
  *
  *   k_conv<CIN, COUT, EPI>  implicit-GEMM convolution with tcgen05.mma
  *       (cta_group::1, kind::f16, M = 128 voxels, N = COUT, K = 16 per MMA):
- *       per output row, for each of the 27 taps the shifted input row
- *       (128 x CIN bf16, zero outside the volume) is fetched by a TMA tensor
- *       load into a ring of shared-memory stages; the 27 weight tiles stay in
- *       shared memory (one TMA load per CTA); the accumulator lives in TMEM
- *       and is read back with tcgen05.ld by four epilogue warps.  Warp roles:
+ *       a tile is CONV_ROWS consecutive output rows of one slice; each input
+ *       row the tile needs (rows y0 - 1 .. y0 + CONV_ROWS of slices z - 1 ..
+ *       z + 1), at each of the three x shifts, is fetched once by a TMA tensor
+ *       load (128 x CIN bf16, zero outside the volume) into a ring of
+ *       shared-memory stages and feeds every output row it is a tap of (up to
+ *       three), 54 boxes per 4 rows instead of 27 per row; the 27 weight tiles
+ *       stay in shared memory (one TMA load per CTA); the tile's CONV_ROWS
+ *       accumulators live in TMEM, two tiles' worth, so that the epilogue
+ *       reads one tile (tcgen05.ld, four epilogue warps) while the next one's
+ *       MMAs run.  Warp roles:
  *       warp 0 TMA producer, warp 1 MMA issuer, warps 2-5 epilogue.  Every
  *       mbarrier wait is bounded (about a second); a timeout sets an error
  *       counter and the CTA finishes without further waits.
@@ -55,6 +60,9 @@ constexpr int CNN_LAYERS = 8;
 constexpr int CNN_TAPS = 27;
 constexpr int CONV_THREADS = 192; /* warp 0 producer, warp 1 MMA, warps 2-5 epilogue */
 constexpr int CONV_STAGES = 6;
+constexpr int CONV_ROWS = 4;   /* output rows (of 128 voxels) per tile */
+constexpr int CONV_ACC = 32;   /* TMEM columns per output row's accumulator (>= COUT) */
+constexpr int CONV_TMEM = 2 * CONV_ROWS * CONV_ACC; /* two tiles' accumulators: 256 columns */
 enum { EPI_RELU = 0, EPI_OUT = 1, EPI_DGRAD = 2 };
 
 /* (c_in, c_out) of each layer as stored (padded) and as defined */
@@ -182,7 +190,7 @@ struct ConvSmem {
     static constexpr int OFF_A = ((B_BYTES + 1023) / 1024) * 1024;
     /* 8 KB after the stages: the MMA's operand reads end well inside the allocation */
     static constexpr int OFF_BAR = OFF_A + CONV_STAGES * A_BYTES + 8192;
-    static constexpr int NBAR = 2 * CONV_STAGES + 3; /* full, empty, weights, tmem full, tmem empty */
+    static constexpr int NBAR = 2 * CONV_STAGES + 5; /* full, empty, weights, tmem full x2, tmem empty x2 */
     static constexpr int TOTAL = OFF_BAR + NBAR * 8 + 16 + 1024; /* + TMEM address slot + alignment slack */
 };
 
@@ -197,74 +205,95 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv(const __grid_constant_
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
     uint64_t* empty = full + CONV_STAGES;
     uint64_t* wbar = empty + CONV_STAGES;
-    uint64_t* tfull = wbar + 1;
-    uint64_t* tempty = tfull + 1;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(tempty + 1);
+    uint64_t* tfull = wbar + 1;  /* [2]: accumulator buffer b complete */
+    uint64_t* tempty = tfull + 2; /* [2]: accumulator buffer b read by the epilogue */
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tempty + 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntiles = p.depth * p.height;
+    /* a tile: CONV_ROWS consecutive output rows y0 .. of one slice z */
+    const int row_groups = (p.height + CONV_ROWS - 1) / CONV_ROWS;
+    const int ntiles = p.depth * row_groups;
     if (threadIdx.x == 0) {
         for (int s = 0; s < CONV_STAGES; ++s) {
             mbar_init(full + s, 1);
             mbar_init(empty + s, 1);
         }
         mbar_init(wbar, 1);
-        mbar_init(tfull, 1);
-        mbar_init(tempty, 4);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(tfull + b, 1);
+            mbar_init(tempty + b, 4);
+        }
         mbar_fence_init();
     }
-    if (warp == 0) tmem_alloc(tslot, 32);
+    if (warp == 0) tmem_alloc(tslot, CONV_TMEM);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
     bool ok = true;
     if (warp == 0) {
-        if (lane == 0) { /* TMA producer */
+        if (lane == 0) { /* TMA producer: per tile the input rows y0 - 1 .. y0 + CONV_ROWS of slices
+                          * z - 1 .. z + 1, each at the three x shifts, one box each */
             mbar_expect_tx(wbar, (uint32_t)L::B_BYTES);
             tma_load_3d(sB, &w_map, 0, 0, 0, wbar);
             uint32_t it = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int z = t / p.height, y = t - z * p.height;
-                for (int tap = 0; tap < CNN_TAPS; ++tap, ++it) {
-                    const int s = (int)(it % CONV_STAGES);
-                    const uint32_t round = it / CONV_STAGES;
-                    if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1u)) {
-                        ok = false;
-                        break;
-                    }
-                    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-                    mbar_expect_tx(full + s, (uint32_t)L::A_BYTES);
-                    tma_load_4d(sA + s * L::A_BYTES, &in_map, 0, dx, y + dy, z + dz, full + s);
-                }
+                const int z = t / row_groups, y0 = (t - z * row_groups) * CONV_ROWS;
+                for (int dz = -1; dz <= 1 && ok; ++dz)
+                    for (int yy = y0 - 1; yy <= y0 + CONV_ROWS && ok; ++yy)
+                        for (int dx = -1; dx <= 1; ++dx, ++it) {
+                            const int s = (int)(it % CONV_STAGES);
+                            const uint32_t round = it / CONV_STAGES;
+                            if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1u)) {
+                                ok = false;
+                                break;
+                            }
+                            mbar_expect_tx(full + s, (uint32_t)L::A_BYTES);
+                            tma_load_4d(sA + s * L::A_BYTES, &in_map, 0, dx, yy, z + dz, full + s);
+                        }
             }
         }
     } else if (warp == 1) {
-        if (lane == 0) { /* MMA issuer */
+        if (lane == 0) { /* MMA issuer: each box feeds the output rows it is a tap of (up to three) */
             constexpr uint32_t idesc = umma_idesc(COUT);
             ok = mbar_wait(wbar, 0);
             uint32_t it = 0, tile = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tile) {
-                if (tile > 0 && !mbar_wait(tempty, (tile - 1) & 1u)) { /* the epilogue has read the accumulator */
+                const uint32_t buf = tile & 1u, use = tile >> 1;
+                if (use > 0 && !mbar_wait(tempty + buf, (use - 1) & 1u)) { /* the epilogue has read buffer buf */
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                for (int tap = 0; tap < CNN_TAPS; ++tap, ++it) {
-                    const int s = (int)(it % CONV_STAGES);
-                    if (!mbar_wait(full + s, (it / CONV_STAGES) & 1u)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint32_t a0 = saddr(sA + s * L::A_BYTES), b0 = saddr(sB + tap * L::B_TAP);
+                const uint32_t acc0 = tmem + buf * (CONV_ROWS * CONV_ACC);
+                const int z = t / row_groups, y0 = (t - z * row_groups) * CONV_ROWS;
+                (void)z;
+                for (int dz = -1; dz <= 1 && ok; ++dz)
+                    for (int yy = y0 - 1; yy <= y0 + CONV_ROWS && ok; ++yy)
+                        for (int dx = -1; dx <= 1; ++dx, ++it) {
+                            const int s = (int)(it % CONV_STAGES);
+                            if (!mbar_wait(full + s, (it / CONV_STAGES) & 1u)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                            const uint32_t a0 = saddr(sA + s * L::A_BYTES);
 #pragma unroll
-                    for (int kk = 0; kk < CIN / 16; ++kk)
-                        umma_bf16(tmem, umma_desc(a0 + kk * 32, L::ROW), umma_desc(b0 + kk * 32, L::ROW), idesc,
-                                  (tap > 0 || kk > 0) ? 1u : 0u);
-                    umma_commit(empty + s); /* the stage is free once these MMAs have read it */
-                }
+                            for (int j = 0; j < CONV_ROWS; ++j) {
+                                const int dy = yy - (y0 + j);
+                                if (dy < -1 || dy > 1) continue;
+                                const int tap = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
+                                const uint32_t b0 = saddr(sB + tap * L::B_TAP);
+                                /* the first contribution to row j: dz = dy = dx = -1 */
+                                const bool first = dz == -1 && dy == -1 && dx == -1;
+#pragma unroll
+                                for (int kk = 0; kk < CIN / 16; ++kk)
+                                    umma_bf16(acc0 + (uint32_t)(j * CONV_ACC), umma_desc(a0 + kk * 32, L::ROW),
+                                              umma_desc(b0 + kk * 32, L::ROW), idesc, (first && kk == 0) ? 0u : 1u);
+                            }
+                            umma_commit(empty + s); /* the stage is free once these MMAs have read it */
+                        }
                 if (!ok) break;
-                umma_commit(tfull);
+                umma_commit(tfull + buf);
             }
         }
     } else { /* epilogue: warps 2-5, TMEM lanes 32 * (warp % 4) .. + 31 */
@@ -272,51 +301,57 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv(const __grid_constant_
         const int x = q * 32 + lane; /* the tile's row = voxel x */
         uint32_t tile = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tile) {
-            if (!mbar_wait(tfull, tile & 1u)) {
+            const uint32_t buf = tile & 1u, use = tile >> 1;
+            if (!mbar_wait(tfull + buf, use & 1u)) {
                 ok = false;
                 break;
             }
             tc_fence_after();
-            uint32_t r[32];
-            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16), r);
-            if (COUT > 16) tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + 16, r + 16);
-            tmem_wait_ld();
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(tempty);
-            const int z = t / p.height, y = t - z * p.height;
-            const size_t v = ((size_t)z * p.height + y) * CNN_W + x;
-            if (EPI == EPI_OUT) {
-                p.out_f[v] = p.x0[v] + (__uint_as_float(r[0]) + p.bias[0]);
-            } else {
-                uint32_t packed[COUT / 2];
-                if (EPI == EPI_RELU) {
+            const int z = t / row_groups, y0 = (t - z * row_groups) * CONV_ROWS;
+            for (int j = 0; j < CONV_ROWS; ++j) {
+                uint32_t r[32];
+                const uint32_t col = buf * (CONV_ROWS * CONV_ACC) + (uint32_t)(j * CONV_ACC);
+                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + col, r);
+                if (COUT > 16) tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + col + 16, r + 16);
+                tmem_wait_ld();
+                const int y = y0 + j;
+                if (y >= p.height) continue;
+                const size_t v = ((size_t)z * p.height + y) * CNN_W + x;
+                if (EPI == EPI_OUT) {
+                    p.out_f[v] = p.x0[v] + (__uint_as_float(r[0]) + p.bias[0]);
+                } else {
+                    uint32_t packed[COUT / 2];
+                    if (EPI == EPI_RELU) {
 #pragma unroll
-                    for (int c = 0; c < COUT; c += 2) {
-                        const float a = fmaxf(__uint_as_float(r[c]) + p.bias[c], 0.0f);
-                        const float b = fmaxf(__uint_as_float(r[c + 1]) + p.bias[c + 1], 0.0f);
-                        packed[c / 2] = (uint32_t)tobf(a) | ((uint32_t)tobf(b) << 16);
-                    }
-                } else { /* EPI_DGRAD */
-                    const uint4* mrow = reinterpret_cast<const uint4*>(p.mask + v * COUT);
-#pragma unroll
-                    for (int c8 = 0; c8 < COUT / 8; ++c8) {
-                        const uint4 m = mrow[c8];
-                        const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
-#pragma unroll
-                        for (int h = 0; h < 4; ++h) {
-                            const int c = c8 * 8 + h * 2;
-                            const float a = bf((uint16_t)(mw[h] & 0xffffu)) > 0.0f ? __uint_as_float(r[c]) : 0.0f;
-                            const float b = bf((uint16_t)(mw[h] >> 16)) > 0.0f ? __uint_as_float(r[c + 1]) : 0.0f;
+                        for (int c = 0; c < COUT; c += 2) {
+                            const float a = fmaxf(__uint_as_float(r[c]) + p.bias[c], 0.0f);
+                            const float b = fmaxf(__uint_as_float(r[c + 1]) + p.bias[c + 1], 0.0f);
                             packed[c / 2] = (uint32_t)tobf(a) | ((uint32_t)tobf(b) << 16);
                         }
-                    }
-                }
-                uint4* orow = reinterpret_cast<uint4*>(p.out_bf + v * COUT);
+                    } else { /* EPI_DGRAD */
+                        const uint4* mrow = reinterpret_cast<const uint4*>(p.mask + v * COUT);
 #pragma unroll
-                for (int c8 = 0; c8 < COUT / 8; ++c8)
-                    orow[c8] = make_uint4(packed[c8 * 4], packed[c8 * 4 + 1], packed[c8 * 4 + 2], packed[c8 * 4 + 3]);
+                        for (int c8 = 0; c8 < COUT / 8; ++c8) {
+                            const uint4 m = mrow[c8];
+                            const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+                            for (int h = 0; h < 4; ++h) {
+                                const int c = c8 * 8 + h * 2;
+                                const float a = bf((uint16_t)(mw[h] & 0xffffu)) > 0.0f ? __uint_as_float(r[c]) : 0.0f;
+                                const float b = bf((uint16_t)(mw[h] >> 16)) > 0.0f ? __uint_as_float(r[c + 1]) : 0.0f;
+                                packed[c / 2] = (uint32_t)tobf(a) | ((uint32_t)tobf(b) << 16);
+                            }
+                        }
+                    }
+                    uint4* orow = reinterpret_cast<uint4*>(p.out_bf + v * COUT);
+#pragma unroll
+                    for (int c8 = 0; c8 < COUT / 8; ++c8)
+                        orow[c8] = make_uint4(packed[c8 * 4], packed[c8 * 4 + 1], packed[c8 * 4 + 2], packed[c8 * 4 + 3]);
+                }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty + buf);
         }
     }
     if (!ok && lane == 0) atomicAdd(p.err, 1ull);
@@ -324,7 +359,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv(const __grid_constant_
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tmem, 32);
+        tmem_dealloc(tmem, CONV_TMEM);
     }
 }
 
@@ -713,7 +748,7 @@ pct_status launch_conv(pct_cnn* n, const CUtensorMap& in, const CUtensorMap& w, 
         PCT_CUDA(cudaFuncSetAttribute(k_conv<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
     }
-    const int tiles = n->depth * n->height;
+    const int tiles = n->depth * ((n->height + CONV_ROWS - 1) / CONV_ROWS);
     const int grid = tiles < 2 * n->sms ? tiles : 2 * n->sms;
     ++n->launches;
     k_conv<CIN, COUT, EPI><<<grid, CONV_THREADS, smem, n->stream>>>(in, w, a);
