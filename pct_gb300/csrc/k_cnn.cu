@@ -255,6 +255,9 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv(const __grid_constant_
     } else if (warp == 1) {
         if (lane == 0) { /* MMA issuer: each box feeds the output rows it is a tap of (up to three) */
             constexpr uint32_t idesc = umma_idesc(COUT);
+            /* descriptors of the first stage and the first tap; the others differ only in the
+             * start address field (address / 16, all offsets multiples of 16 below 256 KB) */
+            const uint64_t da0 = umma_desc(saddr(sA), L::ROW), db0 = umma_desc(saddr(sB), L::ROW);
             ok = mbar_wait(wbar, 0);
             uint32_t it = 0, tile = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tile) {
@@ -276,19 +279,19 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv(const __grid_constant_
                                 break;
                             }
                             tc_fence_after();
-                            const uint32_t a0 = saddr(sA + s * L::A_BYTES);
+                            const uint64_t da = da0 + (uint64_t)((uint32_t)(s * L::A_BYTES) >> 4);
 #pragma unroll
                             for (int j = 0; j < CONV_ROWS; ++j) {
                                 const int dy = yy - (y0 + j);
                                 if (dy < -1 || dy > 1) continue;
                                 const int tap = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
-                                const uint32_t b0 = saddr(sB + tap * L::B_TAP);
+                                const uint64_t db = db0 + (uint64_t)((uint32_t)(tap * L::B_TAP) >> 4);
                                 /* the first contribution to row j: dz = dy = dx = -1 */
                                 const bool first = dz == -1 && dy == -1 && dx == -1;
 #pragma unroll
-                                for (int kk = 0; kk < CIN / 16; ++kk)
-                                    umma_bf16(acc0 + (uint32_t)(j * CONV_ACC), umma_desc(a0 + kk * 32, L::ROW),
-                                              umma_desc(b0 + kk * 32, L::ROW), idesc, (first && kk == 0) ? 0u : 1u);
+                                for (int kk = 0; kk < CIN / 16; ++kk) /* K step: 32 bytes = 2 address units */
+                                    umma_bf16(acc0 + (uint32_t)(j * CONV_ACC), da + (uint64_t)(2 * kk),
+                                              db + (uint64_t)(2 * kk), idesc, (first && kk == 0) ? 0u : 1u);
                             }
                             umma_commit(empty + s); /* the stage is free once these MMAs have read it */
                         }
