@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--train-phantoms", type=int, default=64, help="cfg5: training phantoms")
     ap.add_argument("--eval-phantoms", type=int, default=8, help="cfg5: held-out phantoms")
     ap.add_argument("--train-steps", type=int, default=3000, help="cfg5: Adam steps")
+    ap.add_argument("--warmstart-target", default="drop", choices=["drop", "truth"],
+                    help="cfg5: train towards the pairs' 20-iteration plain DROP images (drop) or, as an extra "
+                         "measurement, towards the phantoms' RSP maps (truth)")
     ap.add_argument("--chord-bf16", type=int, default=None, choices=[0, 1],
                     help="round chords to bfloat16 (default: the workload's setting; cfg4 uses bf16)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -285,7 +288,8 @@ def run_warmstart(a, ws, rank):
     except Exception:
         pass
     with Clocks(0) as clk:
-        res = warmstart.experiment(a.train_phantoms, range(1001, 1001 + a.eval_phantoms), steps=a.train_steps)
+        res = warmstart.experiment(a.train_phantoms, range(1001, 1001 + a.eval_phantoms), steps=a.train_steps,
+                                   target=a.warmstart_target)
     evaluated = len(res["eval_seeds"])
     nv = warmstart.COLS * warmstart.COLS * warmstart.SLICES
     real, padded = warmstart.conv_flops(nv)
@@ -312,10 +316,13 @@ def run_warmstart(a, ws, rank):
            "data": "synthetic (seeded ellipsoid phantoms of the batched-scan generator)",
            "config": {"workload": "cfg5: %d training (of %d seeds tried: targets where plain DROP diverged are "
                                   "skipped) / %d of %d held-out phantoms (the same rule), 128x128x16, %d histories "
-                                  "each, DROP block %d, lambda %.2g, targets = 20 plain DROP iterations, %d Adam steps"
+                                  "each, DROP block %d, lambda %.2g, training targets = %s, %d Adam steps"
                                   % (len(res["train_seeds"]), res["seeds_tried"], evaluated, a.eval_phantoms,
                                      res["histories"],
-                                     res["block_size"], res["lambda"], res["steps"])},
+                                     res["block_size"], res["lambda"],
+                                     "the phantoms' RSP maps (an extra measurement: known for synthetic phantoms "
+                                     "only)" if a.warmstart_target == "truth" else "20 plain DROP iterations",
+                                     res["steps"])},
            "targets": summary, "start_error": start,
            "training": {"pairs_seconds": res["pairs_seconds"], "train_seconds": res["train_seconds"],
                         "seconds_per_step": res["train_seconds"] / res["steps"],

@@ -97,14 +97,16 @@ def curated_pairs(first_seed, count, histories, block_size, target_iterations=20
     return pairs, s - first_seed
 
 
-def train(net, pairs, steps, lr=1e-3, lr_final=1e-4, seed=0, log_every=0):
-    """Adam over randomly drawn pairs (cosine-decayed learning rate); returns the loss per step."""
+def train(net, pairs, steps, lr=1e-3, lr_final=1e-4, seed=0, log_every=0, target_key="target"):
+    """Adam over randomly drawn pairs (cosine-decayed learning rate) towards pair[target_key]
+    ("target": the pair's plain DROP image; "truth": the phantom's RSP map); returns the loss
+    per step."""
     rng = np.random.default_rng(seed)
     losses = []
     for s in range(steps):
         p = pairs[int(rng.integers(len(pairs)))]
         a = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * s / max(steps - 1, 1)))
-        losses.append(net.train_step(p["x0"], p["hull"], p["target"], float(a)))
+        losses.append(net.train_step(p["x0"], p["hull"], p[target_key], float(a)))
         if log_every and s % log_every == 0:
             print("step %d loss %.4g" % (s, losses[-1]), flush=True)
     return losses
@@ -170,10 +172,12 @@ def time_forward(net, pair, reps=20):
 
 def experiment(n_train, eval_seeds, histories=10_000_000, block_size=200000, lam=0.1, target_iterations=20,
                steps=3000, lr=5e-4, eval_iterations=30, net_seed=1, log=None, first_train_seed=2000,
-               curate_eval=True):
+               curate_eval=True, target="drop"):
     """Trains a network on `n_train` curated pairs (seeds from `first_train_seed` on) and
     compares the two starts on `eval_seeds` (with `curate_eval`, on those whose own plain
-    DROP target passes `improved`).
+    DROP target passes `improved`).  `target`: "drop" trains towards the pairs' plain DROP
+    images (the method's own output); "truth" towards the phantoms' RSP maps (known for
+    synthetic phantoms only).
 
     Per held-out seed and start: iterations and wall time (DROP device time, plus the
     network's inference for the learned start) until the voxel RSP RMSE is at or below
@@ -189,7 +193,8 @@ def experiment(n_train, eval_seeds, histories=10_000_000, block_size=200000, lam
     try:
         net.init(net_seed)
         t0 = time.perf_counter()
-        losses = train(net, pairs, steps, lr=lr, lr_final=lr / 10, log_every=log or 0)
+        losses = train(net, pairs, steps, lr=lr, lr_final=lr / 10, log_every=log or 0,
+                       target_key="truth" if target == "truth" else "target")
         t_train = time.perf_counter() - t0
         t_fwd = time_forward(net, pairs[0])
         per_seed = []
@@ -217,6 +222,6 @@ def experiment(n_train, eval_seeds, histories=10_000_000, block_size=200000, lam
         net.close()
     return {"pairs_seconds": t_pairs, "train_seconds": t_train, "forward_seconds": t_fwd, "losses": losses,
             "per_seed": per_seed,
-            "histories": histories, "block_size": block_size, "lambda": lam, "steps": steps,
+            "histories": histories, "block_size": block_size, "lambda": lam, "steps": steps, "training_target": target,
             "train_seeds": [p["seed"] for p in pairs], "seeds_tried": tried,
             "eval_seeds": [r["seed"] for r in per_seed], "eval_seeds_tried": list(eval_seeds)}
